@@ -1,0 +1,113 @@
+/*
+ * sepx.h -- C ABI of the GB300 (sm_103a) acoustic Born / RTM propagation path.
+ *
+ * Part 1 is a drop-in for the reference's GPU interface, Born/gpu_funcs_3d.h:4-27
+ * of SEP_Code: the same eleven extern "C" functions with the same names,
+ * argument order and meaning (host buffers in, host buffers out, one call runs
+ * a whole time loop, module-global device state).  Like the reference they
+ * return void; unlike the reference they never exit() the process: a failure
+ * is recorded and can be read with sepx_last_error().
+ *
+ * Part 2 is the same interface with an int status (0 = success, negative =
+ * error) under the sepx_ prefix, plus device-resident variants that keep the
+ * image, traces and source wavefields in HBM between calls.
+ *
+ * Volumes are float[n3][n2][n1] (axis 1 fastest), traces float[nrec][ntrace],
+ * exactly as the reference lays them out on the host.  One GPU (ngpus == 1);
+ * the reference's multi-GPU z-slab split is not provided.
+ */
+#ifndef SEPX_H
+#define SEPX_H
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- Part 1: reference-named C ABI ---------------- */
+
+/* Born/gpu_funcs_3d.h:7 (gpu_funcs_3d.cu:10-45): select the device(s). */
+void setup_cuda(int ngpus, int argc, char **argv);
+/* Born/gpu_funcs_3d.h:9 (gpu_funcs_3d.cu:133-315): nt+1 steps of the source
+ * wavefield with the random-boundary velocity; with get_last the last two
+ * wavefields are returned in p0 (older) and p1 (newest).  `damp` is ignored,
+ * as in the reference. */
+void source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0, float *p1, int jt,
+                 int npts, int nt);
+/* Born/gpu_funcs_3d.h:11 (gpu_funcs_3d.cu:509-712): receiver back-propagation,
+ * source reconstruction from (p0_s_cpu, p1_s_cpu) and zero-lag image into img. */
+void rtm_adjoint(int n1, int n2, int n3, int j, float *p0_s_cpu, float *p1_s_cpu, float *img,
+                 int npts, int nt);
+/* Born/gpu_funcs_3d.h:13 (gpu_funcs_3d.cu:317-505): Born modelling over img;
+ * traces accumulate onto the receiver buffer given to transfer_receiver_func
+ * and are returned in dat (nt_big samples per receiver). */
+void rtm_forward(int n1, int n2, int n3, int jt, float *img, float *dat, int npts_src, int nt,
+                 int nt_big, int nx, int ny);
+/* Born/gpu_funcs_3d.h:15 (gpu_funcs_3d.cu:714-723): ns source sinc rows. */
+void transfer_sinc_table_s(int nsinc, int ns, float **tables);
+/* Born/gpu_funcs_3d.h:17 (gpu_funcs_3d.cu:725-733): ns receiver sinc rows. */
+void transfer_sinc_table_d(int nsinc, int ns, float **tabled);
+/* Born/gpu_funcs_3d.h:19 (gpu_funcs_3d.cu:735-745): source points (linear cell
+ * index) and their traces float[npts][nt]. */
+void transfer_source_func(int npts, int nt, int *locs, float *vals);
+/* Born/gpu_funcs_3d.h:21 (gpu_funcs_3d.cu:747-758): receiver points and their
+ * traces float[nx*ny][nt]. */
+void transfer_receiver_func(int nx, int ny, int nt, int *locs, float *vals);
+/* Born/gpu_funcs_3d.h:23 (gpu_funcs_3d.cu:761-767): v^2 dt^2 on the padded grid. */
+void transfer_vel_func1(int nx, int ny, int nz, float *vel);
+/* Born/gpu_funcs_3d.h:25 (gpu_funcs_3d.cu:769-775): second velocity; the
+ * reference uploads it but no kernel reads it, so it is checked and dropped. */
+void transfer_vel_func2(int nx, int ny, int nz, float *vel);
+/* Born/gpu_funcs_3d.h:27 (gpu_funcs_3d.cu:777-803): grid spacing, sponge
+ * (bc_a, bc_b) and padded grid; allocates the device volumes. */
+void create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b, float bc_b_y, int nx,
+                      int ny, int nz);
+
+/* ---------------- Part 2: status-returning interface ---------------- */
+
+int sepx_setup_cuda(int ngpus);
+int sepx_create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b, float bc_b_y,
+                          int nx, int ny, int nz);
+int sepx_transfer_sinc_table_s(int nsinc, int ns, float **tables);
+int sepx_transfer_sinc_table_d(int nsinc, int ns, float **tables);
+int sepx_transfer_source_func(int npts, int nt, const int *locs, const float *vals);
+int sepx_transfer_receiver_func(int nx, int ny, int nt, const int *locs, const float *vals);
+int sepx_transfer_vel_func1(int nx, int ny, int nz, const float *vel);
+int sepx_transfer_vel_func2(int nx, int ny, int nz, const float *vel);
+int sepx_source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0, float *p1,
+                     int jt, int npts, int nt);
+int sepx_rtm_forward(int n1, int n2, int n3, int jt, const float *img, float *dat, int npts_src,
+                     int nt, int nt_big, int nx, int ny);
+int sepx_rtm_adjoint(int n1, int n2, int n3, int jt, const float *p0_s, const float *p1_s,
+                     float *img, int npts, int nt);
+
+/* Device-resident variants: enqueue the time loop on the context stream and
+ * return without synchronising.  source_prop keeps its last two wavefields in
+ * HBM; rtm_forward reads the image set by sepx_set_image and accumulates into
+ * the receiver buffer; rtm_adjoint images into the image buffer, starting
+ * from the last source_prop wavefields (use_source_last != 0) or from the ones
+ * set with sepx_set_source_fields. */
+int sepx_source_prop_resident(int jt, int npts, int nt);
+int sepx_rtm_forward_resident(int jt, int npts_src, int nt);
+int sepx_rtm_adjoint_resident(int jt, int npts, int nt, int use_source_last);
+int sepx_set_image(const float *img);                 /* host, dense */
+int sepx_get_image(float *img);                       /* host, dense */
+int sepx_set_source_fields(const float *p0, const float *p1);
+int sepx_get_source_fields(float *p0, float *p1);
+int sepx_set_traces(const float *vals);               /* [nrec][ntrace] */
+int sepx_get_traces(float *vals);
+int sepx_zero_traces(void);                          /* receiver buffer := 0 on the device */
+int sepx_synchronize(void);
+void *sepx_get_stream(void);          /* the cudaStream_t every call enqueues on */
+
+/* Diagnostics and tuning. */
+const char *sepx_last_error(void);
+int sepx_device_error(void);          /* device error word (bounded waits), then cleared */
+long long sepx_kernel_launches(void); /* kernels launched by this library so far */
+int sepx_set_zchunk(int planes);      /* z planes per CTA; 0 = automatic */
+int sepx_reset(void);                 /* free every device buffer */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,458 @@
+// sepx_prop.cu -- fused 8th-order acoustic propagation steps for sm_103a.
+//
+// One launch advances one or two wavefields by one time step over the updated
+// interior of the padded grid and applies, in the same pass, everything the
+// reference does to those cells in that step with separate launches
+// (Born/gpu_funcs_3d.cu:398-471 and :600-675): sponge damping, source and
+// receiver injection, Born scattering, zero-lag imaging and receiver
+// extraction.  Per cell it moves the compulsory bytes only (read previous,
+// current and v^2dt^2 once, write the new field once); halo cells come from
+// shared memory / L2.
+//
+// Structure of one CTA (tile of 32 x 16 cells, a chunk of z planes):
+//  * warp 4, lane 0 is the producer: for every plane it issues TMA box loads
+//    (cp.async.bulk.tensor) of the current field with a 4-cell halo, the
+//    previous field, v^2dt^2, the image and the current field 4 planes ahead,
+//    into a ring of STAGES shared-memory stages guarded by mbarriers;
+//  * warps 0-3 consume: each thread owns 4 consecutive x cells (one float4),
+//    keeps a 9-deep register queue of the current field along z and reads the
+//    x/y neighbours from the staged halo tile;
+//  * the sponge is applied when a value is written (the reference damps the
+//    current and previous fields in place before each step; multiplying the
+//    new field once per sponge pass at write time and the previous field the
+//    same number of extra times reproduces its sequence of float multiplies
+//    without touching halo cells).
+//
+// Arithmetic follows the oracle's contract term for term (explicit
+// __fmaf_rn / __fmul_rn / __fadd_rn, no contraction freedom), so a step is
+// bit-identical to the CPU restatement.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "sepx_device.cuh"
+#include "sepx_prop.h"
+
+namespace sepx {
+
+template <int MODE>
+struct Mode {
+  static constexpr int NF = (MODE == kBornFwd || MODE == kRtmAdj) ? 2 : 1;
+  static constexpr bool F0_VEL_INSIDE = (MODE == kBornFwd);   // wave_kernel_adj
+  static constexpr bool VEL_HALO = F0_VEL_INSIDE;
+  static constexpr bool HAS_IMG = (MODE != kSrcProp);
+  static constexpr bool HAS_AUX = (MODE == kRtmAdj1);
+  // sponge passes per step on each field (write-time multiplies, extra
+  // multiplies of the previous field)
+  static constexpr int KW0 = (MODE == kBornFwd) ? 2 : ((MODE == kSrcProp) ? 0 : 1);
+  static constexpr int KW1 = (MODE == kBornFwd) ? 1 : 0;
+  static constexpr bool SRC_INJ = (MODE == kSrcProp || MODE == kBornFwd);
+  static constexpr int SRC_FIELD = (MODE == kSrcProp) ? 0 : 1;
+  static constexpr bool REC_EXTRACT = (MODE == kBornFwd);
+  static constexpr bool REC_INJECT = (MODE == kRtmAdj || MODE == kRtmAdj1);
+  // stage layout (floats)
+  static constexpr int FEED = 0;
+  static constexpr int FEEDV = FEED + NF * kCenterFloats;
+  static constexpr int HALO = FEEDV + (VEL_HALO ? kCenterFloats : 0);
+  static constexpr int VELT = HALO + NF * kHaloFloats;
+  static constexpr int PREV = VELT + (VEL_HALO ? kHaloFloats : kCenterFloats);
+  static constexpr int IMG = PREV + NF * kCenterFloats;
+  static constexpr int AUX = IMG + (HAS_IMG ? kCenterFloats : 0);
+  static constexpr int STAGE = AUX + (HAS_AUX ? kCenterFloats : 0);
+  static constexpr uint32_t BYTES_NOIMG =
+      4u * (NF * kCenterFloats + (VEL_HALO ? kCenterFloats : 0) + NF * kHaloFloats +
+            (VEL_HALO ? kHaloFloats : kCenterFloats) + NF * kCenterFloats +
+            (HAS_AUX ? kCenterFloats : 0));
+  static constexpr uint32_t BYTES_IMG = BYTES_NOIMG + (HAS_IMG ? 4u * kCenterFloats : 0u);
+};
+
+// Sponge factor of damp_kernel (Born/wave_fkernel.3d8o.cu:183-210), one GPU:
+// cells with x < xg, y < yg and edge = distance to the nearest face minus 4
+// >= 0; 1 elsewhere.
+__device__ __forceinline__ float sponge(const PropParams &P, int x, int y, int z) {
+  const PropGeom &g = P.g;
+  if (x >= g.xg || y >= g.yg) return 1.0f;
+  int e = x - 4;
+  e = min(e, z - 4);
+  e = min(e, g.n2 - 4 - y);
+  e = min(e, g.n1 - 4 - x);
+  e = min(e, g.n3 - 4 - z);
+  e = min(e, y - 4);
+  if (e < 0 || e >= P.ntab) return 1.0f;
+  return __ldg(P.damp_tab + e);
+}
+
+template <int K>
+__device__ __forceinline__ float damp_k(float v, float t) {
+#pragma unroll
+  for (int k = 0; k < K; k++) v = __fmul_rn(v, t);
+  return v;
+}
+
+// Laplacian part of wave_kernel (vel outside): s = c0 p + sum_k pairs.
+// xw: x-4 .. x+7 of the row, ym/yp: rows y-k / y+k, qz: z-queue (plane z-4+j).
+__device__ __forceinline__ void lap_plain(const float *coef, const float (&xw)[12],
+                                          const float4 (&ym)[4], const float4 (&yp)[4],
+                                          const float4 (&qz)[9], float (&s)[4]) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float p = xw[4 + c];
+    float acc = __fmul_rn(coef[0], p);
+#pragma unroll
+    for (int k = 1; k <= 4; k++) {
+      acc = __fmaf_rn(coef[3 * k - 2], __fadd_rn(xw[4 + c + k], xw[4 + c - k]), acc);
+      acc = __fmaf_rn(coef[3 * k - 1], __fadd_rn(comp(yp[k - 1], c), comp(ym[k - 1], c)), acc);
+      acc = __fmaf_rn(coef[3 * k], __fadd_rn(comp(qz[4 + k], c), comp(qz[4 - k], c)), acc);
+    }
+    s[c] = acc;
+  }
+}
+
+// Laplacian of (v p), wave_kernel_adj (vel inside): centre (c0 p) v, pairs of
+// rounded products; qz holds the products p v along z.
+__device__ __forceinline__ void lap_velin(const float *coef, const float (&xw)[12],
+                                          const float (&vw)[12], const float4 (&ym)[4],
+                                          const float4 (&yp)[4], const float4 (&vym)[4],
+                                          const float4 (&vyp)[4], const float4 (&qz)[9],
+                                          float (&s)[4]) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float acc = __fmul_rn(__fmul_rn(coef[0], xw[4 + c]), vw[4 + c]);
+#pragma unroll
+    for (int k = 1; k <= 4; k++) {
+      float px = __fadd_rn(__fmul_rn(xw[4 + c + k], vw[4 + c + k]),
+                           __fmul_rn(xw[4 + c - k], vw[4 + c - k]));
+      acc = __fmaf_rn(coef[3 * k - 2], px, acc);
+      float py = __fadd_rn(__fmul_rn(comp(yp[k - 1], c), comp(vyp[k - 1], c)),
+                           __fmul_rn(comp(ym[k - 1], c), comp(vym[k - 1], c)));
+      acc = __fmaf_rn(coef[3 * k - 1], py, acc);
+      acc = __fmaf_rn(coef[3 * k], __fadd_rn(comp(qz[4 + k], c), comp(qz[4 - k], c)), acc);
+    }
+    s[c] = acc;
+  }
+}
+
+__device__ __forceinline__ void load_window(const float *h, float (&w)[12], float4 (&ym)[4],
+                                            float4 (&yp)[4]) {
+  float4 a = lds4(h), b = lds4(h + 4), c = lds4(h + 8);
+  w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+  w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
+  w[8] = c.x; w[9] = c.y; w[10] = c.z; w[11] = c.w;
+#pragma unroll
+  for (int k = 1; k <= 4; k++) {
+    ym[k - 1] = lds4(h + 4 - k * kHX);
+    yp[k - 1] = lds4(h + 4 + k * kHX);
+  }
+}
+
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) {
+  return make_float4(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z),
+                     __fmul_rn(a.w, b.w));
+}
+
+template <int MODE, int STAGES>
+__global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_constant__ PropParams P) {
+  using M = Mode<MODE>;
+  constexpr int NF = M::NF;
+  // dynamic shared memory only: [<=127 B pad][STAGES stages][full bars][empty bars]
+  extern __shared__ unsigned char smem_raw[];
+  float *smem = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                          ~static_cast<uintptr_t>(127));
+  unsigned long long *bar_full = reinterpret_cast<unsigned long long *>(smem + STAGES * M::STAGE);
+  unsigned long long *bar_empty = bar_full + STAGES;
+
+  const PropGeom &g = P.g;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int x0 = g.xb + kTX * blockIdx.x;
+  const int y0 = g.yb + kTY * blockIdx.y;
+  const int za = g.zb + g.zchunk * blockIdx.z;
+  const int niter = min(g.zchunk, g.ze - za);
+  if (niter <= 0) return;   // uniform for the CTA
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), kConsumerThreads / 32);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  const bool load_img = M::HAS_IMG && (MODE == kBornFwd ? P.do_scatter : P.do_image);
+  const uint32_t stage_bytes = load_img ? M::BYTES_IMG : M::BYTES_NOIMG;
+  int issued = 0;
+
+  if (warp == kConsumerThreads / 32) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      for (int f = 0; f < NF; f++) {
+        prefetch_tmap(&P.tm_cur_h[f]);
+        prefetch_tmap(&P.tm_cur_c[f]);
+        prefetch_tmap(&P.tm_prev_c[f]);
+      }
+      for (int i = 0; i < niter; i++) {
+        const int s = i % STAGES;
+        if (i >= STAGES) {
+          if (!mbar_wait_bounded(smem_u32(&bar_empty[s]), ((i / STAGES) - 1) & 1, P.err,
+                                 kErrEmptyWait))
+            break;
+        }
+        const uint32_t fb = smem_u32(&bar_full[s]);
+        mbar_arrive_expect_tx(fb, stage_bytes);
+        float *st = smem + s * M::STAGE;
+        const int z = za + i;
+        for (int f = 0; f < NF; f++)
+          tma_load_3d(smem_u32(st + M::FEED + f * kCenterFloats), &P.tm_cur_c[f], x0, y0, z + 4, fb);
+        if (M::VEL_HALO) tma_load_3d(smem_u32(st + M::FEEDV), &P.tm_vel_c, x0, y0, z + 4, fb);
+        for (int f = 0; f < NF; f++)
+          tma_load_3d(smem_u32(st + M::HALO + f * kHaloFloats), &P.tm_cur_h[f], x0 - kHalo,
+                      y0 - kHalo, z, fb);
+        if (M::VEL_HALO)
+          tma_load_3d(smem_u32(st + M::VELT), &P.tm_vel_h, x0 - kHalo, y0 - kHalo, z, fb);
+        else
+          tma_load_3d(smem_u32(st + M::VELT), &P.tm_vel_c, x0, y0, z, fb);
+        for (int f = 0; f < NF; f++)
+          tma_load_3d(smem_u32(st + M::PREV + f * kCenterFloats), &P.tm_prev_c[f], x0, y0, z, fb);
+        if (load_img) tma_load_3d(smem_u32(st + M::IMG), &P.tm_img_c, x0, y0, z, fb);
+        if (M::HAS_AUX) tma_load_3d(smem_u32(st + M::AUX), &P.tm_aux_c, x0, y0, z, fb);
+        issued = i + 1;
+      }
+    }
+  } else {
+    // ---------------- consumers ----------------
+    const int row = tid >> 3, xq = tid & 7;
+    const int x = x0 + 4 * xq, y = y0 + row;
+    const bool active = (x < g.xe);
+    const long long rowoff = (long long)x + (long long)g.pitch * y;
+    float4 q[NF][9];
+    // warm-up: planes za-4 .. za+3 of the current field(s) along z
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const long long off = rowoff + g.plane * (za - 4 + j);
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          float4 p = ldg4(P.cur[f] + off);
+          if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, ldg4(P.vel + off));
+          q[f][j] = p;
+        }
+      }
+    }
+    const int hoff = (kHalo + row) * kHX + 4 * xq;   // halo tile: column of x-4
+    const int coff = row * kTX + 4 * xq;             // centre tile
+    for (int i = 0; i < niter; i++) {
+      const int s = i % STAGES;
+      if (!mbar_wait_bounded(smem_u32(&bar_full[s]), (i / STAGES) & 1, P.err, kErrFullWait))
+        break;
+      const float *st = smem + s * M::STAGE;
+      const int z = za + i;
+      float res[NF][4];
+      float4 prevv[NF], velc, imgv = make_float4(0.f, 0.f, 0.f, 0.f), auxv;
+      float vwc[4];
+      if (active) {
+        // z-queue feed: plane z+4
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          float4 p = lds4(st + M::FEED + f * kCenterFloats + coff);
+          if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, lds4(st + M::FEEDV + coff));
+          q[f][8] = p;
+        }
+        float vw[12];
+        float4 vym[4], vyp[4];
+        if (M::VEL_HALO) {
+          load_window(st + M::VELT + hoff, vw, vym, vyp);
+          velc = make_float4(vw[4], vw[5], vw[6], vw[7]);
+        } else {
+          velc = lds4(st + M::VELT + coff);
+        }
+        vwc[0] = velc.x; vwc[1] = velc.y; vwc[2] = velc.z; vwc[3] = velc.w;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          float xw[12];
+          float4 ym[4], yp[4];
+          load_window(st + M::HALO + f * kHaloFloats + hoff, xw, ym, yp);
+          float sl[4];
+          if (f == 0 && M::F0_VEL_INSIDE) {
+            lap_velin(P.coef, xw, vw, ym, yp, vym, vyp, q[f], sl);
+#pragma unroll
+            for (int c = 0; c < 4; c++) res[f][c] = __fadd_rn(__fadd_rn(sl[c], xw[4 + c]), xw[4 + c]);
+          } else {
+            lap_plain(P.coef, xw, ym, yp, q[f], sl);
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+              res[f][c] = __fadd_rn(__fmaf_rn(vwc[c], sl[c], xw[4 + c]), xw[4 + c]);
+          }
+          prevv[f] = lds4(st + M::PREV + f * kCenterFloats + coff);
+        }
+        if (load_img) imgv = lds4(st + M::IMG + coff);
+        if (M::HAS_AUX) auxv = lds4(st + M::AUX + coff);
+      }
+      // the stage is no longer read: hand it back to the producer
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&bar_empty[s]));
+
+      if (active) {
+        float t[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) t[c] = (M::KW0 > 0 || M::KW1 > 0) ? sponge(P, x + c, y, z) : 1.f;
+        float val[NF][4];
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          const int kp = (f == 0) ? M::KW0 : M::KW1;
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            float pv = comp(prevv[f], c);
+            if (kp == 1) pv = damp_k<1>(pv, t[c]);
+            if (kp == 2) pv = damp_k<2>(pv, t[c]);
+            val[f][c] = __fsub_rn(res[f][c], pv);
+          }
+        }
+        const long long cell = rowoff + g.plane * z;
+        // source injection into the new field (ids in ascending order)
+        if (M::SRC_INJ && P.src.plane_slot) {
+          const int slot = __ldg(P.src.plane_slot + z);
+          if (slot >= 0) {
+            const int *mp = P.src.map + (long long)slot * g.n1 * g.n2 + (long long)y * g.n1 + x;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              for (int id = __ldg(mp + c); id >= 0; id = __ldg(P.src.next + id))
+                val[M::SRC_FIELD][c] = __fadd_rn(val[M::SRC_FIELD][c], __ldg(P.inj_s + id));
+            }
+          }
+        }
+        // receiver injection (adjoint): time-major traces, 8 taps
+        if (M::REC_INJECT && P.rec.plane_slot) {
+          const int slot = __ldg(P.rec.plane_slot + z);
+          if (slot >= 0) {
+            const int *mp = P.rec.map + (long long)slot * g.n1 * g.n2 + (long long)y * g.n1 + x;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              for (int id = __ldg(mp + c); id >= 0; id = __ldg(P.rec.next + id)) {
+                const float *tr = P.trc + (long long)P.trc_id * P.nrec + id;
+                float acc = __fmul_rn(__ldg(P.sinc_row), __ldg(tr));
+#pragma unroll
+                for (int k = 1; k < 8; k++)
+                  acc = __fmaf_rn(__ldg(P.sinc_row + k), __ldg(tr + (long long)k * P.nrec), acc);
+                val[0][c] = __fadd_rn(val[0][c], acc);
+              }
+            }
+          }
+        }
+        const float s6 = (float)0.000001;
+        if (MODE == kBornFwd) {
+          // Born scattering: rec += 1e-6 src img over x < xg, y < yg
+          if (P.do_scatter && y < g.yg) {
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+              if (x + c < g.xg)
+                val[0][c] = __fmaf_rn(__fmul_rn(s6, val[1][c]), comp(imgv, c), val[0][c]);
+          }
+          // receiver extraction from the new scattered field
+          const int slot = P.rec.plane_slot ? __ldg(P.rec.plane_slot + z) : -1;
+          if (slot >= 0) {
+            const int *mp = P.rec.map + (long long)slot * g.n1 * g.n2 + (long long)y * g.n1 + x;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              for (int id = __ldg(mp + c); id >= 0; id = __ldg(P.rec.next + id)) {
+                float *tr = P.trc + (long long)P.trc_id * P.nrec + id;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                  float *a = tr + (long long)k * P.nrec;
+                  *a = __fmaf_rn(val[0][c], __ldg(P.sinc_row + k), *a);
+                }
+              }
+            }
+          }
+        }
+        if (MODE == kRtmAdj || MODE == kRtmAdj1) {
+          if (P.do_image && y < g.yg) {
+            float4 src = (MODE == kRtmAdj) ? make_float4(val[1][0], val[1][1], val[1][2], val[1][3])
+                                           : auxv;
+            float o[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              float iv = comp(imgv, c);
+              o[c] = (x + c < g.xg) ? __fmaf_rn(__fmul_rn(s6, val[0][c]), comp(src, c), iv) : iv;
+            }
+            *reinterpret_cast<float4 *>(P.img + cell) = make_float4(o[0], o[1], o[2], o[3]);
+          }
+        }
+        // write the new fields with the sponge applied
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          const int kw = (f == 0) ? M::KW0 : M::KW1;
+          float o[4];
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            float v = val[f][c];
+            if (kw == 1) v = damp_k<1>(v, t[c]);
+            if (kw == 2) v = damp_k<2>(v, t[c]);
+            o[c] = v;
+          }
+          stcs4(P.out[f] + cell, make_float4(o[0], o[1], o[2], o[3]));
+        }
+        // advance the z-queues
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+#pragma unroll
+          for (int j = 0; j < 8; j++) q[f][j] = q[f][j + 1];
+      }
+    }
+  }
+
+  // Drain: never leave the CTA with bulk copies still writing its shared memory.
+  __syncthreads();
+  if (warp == kConsumerThreads / 32 && lane == 0) {
+    for (int i = max(0, issued - STAGES); i < issued; i++) {
+      if (!mbar_wait_bounded(smem_u32(&bar_full[i % STAGES]), (i / STAGES) & 1, P.err,
+                             kErrDrainWait))
+        break;
+    }
+  }
+}
+
+template <int MODE, int STAGES>
+constexpr size_t smem_bytes_of() {
+  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 128;
+}
+
+template <int MODE, int STAGES>
+static cudaError_t launch_mode(const PropParams &P, dim3 grid, cudaStream_t st) {
+  const size_t smem = smem_bytes_of<MODE, STAGES>();
+  auto kern = prop_step_kernel<MODE, STAGES>;
+  static bool attr_done = false;   // per instantiation
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  kern<<<grid, kThreads, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
+// Host entry: launch one fused step.
+cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
+  const PropGeom &g = P.g;
+  const int wx = g.xe - g.xb, wy = g.ye - g.yb, wz = g.ze - g.zb;
+  if (wx <= 0 || wy <= 0 || wz <= 0) return cudaSuccess;
+  dim3 grid((wx + kTX - 1) / kTX, (wy + kTY - 1) / kTY, (wz + g.zchunk - 1) / g.zchunk);
+  switch (mode) {
+    case kSrcProp: return launch_mode<kSrcProp, 4>(P, grid, st);
+    case kBornFwd: return launch_mode<kBornFwd, 3>(P, grid, st);
+    case kRtmAdj: return launch_mode<kRtmAdj, 3>(P, grid, st);
+    case kRtmAdj1: return launch_mode<kRtmAdj1, 3>(P, grid, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+size_t prop_smem_bytes(int mode) {
+  switch (mode) {
+    case kSrcProp: return smem_bytes_of<kSrcProp, 4>();
+    case kBornFwd: return smem_bytes_of<kBornFwd, 3>();
+    case kRtmAdj: return smem_bytes_of<kRtmAdj, 3>();
+    case kRtmAdj1: return smem_bytes_of<kRtmAdj1, 3>();
+  }
+  return 0;
+}
+
+}  // namespace sepx

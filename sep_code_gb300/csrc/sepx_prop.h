@@ -1,0 +1,77 @@
+// sepx_prop.h -- parameter block shared by the host driver and the fused
+// propagation kernels (sepx_prop.cu).
+#pragma once
+#include <cuda.h>
+#include <stdint.h>
+
+namespace sepx {
+
+// Tile of one CTA: 32 x 16 cells in (x, y), streaming along z.
+constexpr int kTX = 32;
+constexpr int kTY = 16;
+constexpr int kHalo = 4;                                   // stencil radius
+constexpr int kHX = kTX + 2 * kHalo;                       // 40
+constexpr int kHY = kTY + 2 * kHalo;                       // 24
+constexpr int kCenterFloats = kTX * kTY;                   // 512 (2 KB)
+constexpr int kHaloFloats = kHX * kHY;                     // 960 (3840 B)
+constexpr int kConsumerThreads = 128;                      // 4 cells (one float4) each
+constexpr int kThreads = kConsumerThreads + 32;            // + one TMA producer warp
+
+// Propagation step kinds (one kernel instantiation each):
+//  kSrcProp  source_prop step: source field, vel outside the Laplacian, no
+//            sponge, source injected into the new field
+//  kBornFwd  rtm_forward step: scattered field (vel inside the Laplacian,
+//            sponge twice) + source field (sponge once), source injection,
+//            Born scattering, receiver extraction
+//  kRtmAdj   rtm_adjoint step: receiver field (sponge once) + source field
+//            rebuilt backwards (no sponge), receiver injection, imaging
+//  kRtmAdj1  first rtm_adjoint step: receiver field only, imaging against the
+//            given last source wavefield
+enum PropMode : int { kSrcProp = 0, kBornFwd = 1, kRtmAdj = 2, kRtmAdj1 = 3 };
+
+// Cells that carry sources or receivers, indexed by z plane so the kernel
+// tests a single flag per plane.
+struct PointMap {
+  const int *plane_slot;   // [n3]: -1, or the slot of this plane's map
+  const int *map;          // [nslot][n2][n1]: first point id at the cell, or -1
+  const int *next;         // [npts]: next point id at the same cell, or -1
+};
+
+struct PropGeom {
+  int n1, n2, n3;          // padded grid (the reference's sizes)
+  int pitch;               // row pitch in floats (multiple of 32)
+  long long plane;         // pitch * n2
+  int xb, xe, yb, ye, zb, ze;   // updated interior [b, e)
+  int xg, yg;              // sponge / imaging region: x < xg, y < yg
+  int zchunk;              // planes per CTA along z
+};
+
+struct alignas(64) PropParams {
+  CUtensorMap tm_cur_h[2];    // current field, (kHX x kHY) halo box
+  CUtensorMap tm_cur_c[2];    // current field, (kTX x kTY) box (z-queue feed)
+  CUtensorMap tm_prev_c[2];   // previous field (overwritten by the new one)
+  CUtensorMap tm_vel_h;       // v^2 dt^2, halo box
+  CUtensorMap tm_vel_c;       // v^2 dt^2, centre box
+  CUtensorMap tm_img_c;       // image / reflectivity
+  CUtensorMap tm_aux_c;       // kRtmAdj1: the source wavefield used for imaging
+  PropGeom g;
+  float coef[13];
+  const float *damp_tab;      // sponge factor by edge distance
+  int ntab;
+  const float *cur[2];        // logical-origin pointers (z-queue warm-up loads)
+  const float *vel;
+  float *out[2];              // new fields (the previous-field buffers)
+  float *img;                 // image written back (kRtmAdj, kRtmAdj1)
+  PointMap src;               // source points
+  const float *inj_s;         // per-step injection values, row of this step
+  PointMap rec;               // receiver points
+  float *trc;                 // time-major receiver traces [ntrace][nrec]
+  int nrec;
+  int trc_id;                 // first coarse sample touched this step (it/jt)
+  const float *sinc_row;      // 8 receiver interpolation taps of this step
+  int do_scatter;             // Born scattering this step (it % jt == 0)
+  int do_image;               // imaging this step (it % jt == 0)
+  int *err;                   // device error word
+};
+
+}  // namespace sepx
