@@ -296,3 +296,108 @@ class RefHost:
         rc = self.lib.ref_cg_solve(A, A.shape[0], A.shape[1], np.ascontiguousarray(d, np.float32),
                                    niter, m, C.byref(rr))
         return m, rr.value, rc
+
+
+class RefOperator:
+    """The reference's rtm_zero_op driven end to end on the CPU: its own host
+    classes (SEP files replaced by in-memory buffers) with the oracle loops
+    standing in for the GPU C ABI (oracle/ref_stubs/ref_gpu_stubs.cpp)."""
+
+    def __init__(self, host: "RefHost"):
+        L = self.lib = host.lib
+        L.ref_file_put.argtypes = [C.c_char_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_long]
+        L.ref_param_put.argtypes = [C.c_char_p, C.c_char_p]
+        L.ref_file_size.argtypes = [C.c_char_p]
+        L.ref_file_size.restype = C.c_long
+        L.ref_file_get.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
+        L.ref_file_get.restype = C.c_long
+        L.ref_log_count.restype = C.c_int
+        L.ref_log_entry.argtypes = [C.c_int, C.c_char_p, C.POINTER(C.c_long),
+                                    C.POINTER(C.c_double)]
+        L.ref_log_entry.restype = C.c_int
+        L.ref_last_array.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
+        L.ref_last_array.restype = C.c_long
+
+    def put(self, tag, arr, n, o, d):
+        n = np.asarray(n, np.int32)
+        o = np.asarray(o, np.float32)
+        d = np.asarray(d, np.float32)
+        a = np.ascontiguousarray(arr, np.float32)
+        self._keep = (n, o, d, a)
+        self.lib.ref_file_put(tag.encode(), len(n), n.ctypes.data, o.ctypes.data, d.ctypes.data,
+                              a.ctypes.data, a.nbytes)
+
+    def param(self, name, value):
+        self.lib.ref_param_put(name.encode(), str(value).encode())
+
+    def get(self, tag):
+        n = self.lib.ref_file_size(tag.encode())
+        out = np.zeros(max(n, 0) // 4, np.float32)
+        if n > 0:
+            self.lib.ref_file_get(tag.encode(), out.ctypes.data, n)
+        return out
+
+    def setup(self, s, data=None):
+        """In-memory SEP files and parameters for a Survey-like object ``s``."""
+        self.lib.ref_reset()
+        self.lib.ref_log_clear()
+        rnx, rny, ro2, rd2, ro3, rd3 = s.rec
+        sx, sy, sz = s.shots[0]
+        for k, v in dict(bc_a=s.bc_a, bc_b=s.bc_b, nbound=s.nbound, src_depth=sz,
+                         rec_depth=s.rec_depth, n_gpus=1, aper=8.0).items():
+            self.param(k, repr(float(v)) if isinstance(v, float) else v)
+        m3, m2, m1 = s.vel.shape
+        dd = [float(v) for v in s.spacing]
+        if data is None:
+            data = np.zeros((rny, rnx, s.data_nt), np.float32)
+        self.put("data", data, [s.data_nt, rnx, rny, 1, 1], [0.0, ro2, ro3, sx, sy],
+                 [s.data_dt, rd2, rd3, 1.0, 1.0])
+        self.put("wavelet", s.wavelet, [len(s.wavelet)], [0.0], [s.dtw])
+        self.put("velocity", s.vel, [m1, m2, m3], [0, 0, 0], dd)
+        self.put("image", s.refl, [m1, m2, m3], [0, 0, 0], dd)
+        self.put("mute", np.ones_like(s.refl), [m1, m2, m3], [0, 0, 0], dd)
+
+    def born_forward(self, s):
+        import os
+        import tempfile
+        self.setup(s)
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as td:   # oc_float::make_temp writes files
+            os.chdir(td)
+            try:
+                self.lib.ref_run_born_forward()
+            finally:
+                os.chdir(cwd)
+        rnx, rny = s.rec[0], s.rec[1]
+        return self.get("dataout").reshape(rny, rnx, s.data_nt)
+
+    def rtm_adjoint(self, s, data):
+        import os
+        import tempfile
+        self.setup(s, data=data)
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as td:
+            os.chdir(td)
+            try:
+                self.lib.ref_run_rtm_adjoint()
+            finally:
+                os.chdir(cwd)
+        m3, m2, m1 = s.vel.shape
+        return self.get("image").reshape(m3, m2, m1)
+
+    def log(self):
+        out = []
+        name = C.create_string_buffer(64)
+        ia = (C.c_long * 16)()
+        fa = (C.c_double * 8)()
+        for i in range(self.lib.ref_log_count()):
+            k = self.lib.ref_log_entry(i, name, ia, fa)
+            out.append((name.value.decode(), list(ia)[:k]))
+        return out
+
+    def last_array(self, which, dtype=np.float32):
+        n = self.lib.ref_last_array(which.encode(), None, 0)
+        out = np.zeros(n // 4, dtype)
+        self.lib.ref_last_array(which.encode(), out.ctypes.data, n)
+        return out
