@@ -90,6 +90,18 @@ int sepx_rtm_adjoint(int n1, int n2, int n3, int jt, const float *p0_s, const fl
 int sepx_source_prop_resident(int jt, int npts, int nt);
 int sepx_rtm_forward_resident(int jt, int npts_src, int nt);
 int sepx_rtm_adjoint_resident(int jt, int npts, int nt, int use_source_last);
+/* Linearised Born pair (the operator of least-squares RTM, rtm_zero_op's
+ * forward/adjoint): the source pass stores the source wavefield every js steps
+ * (prec 0 = FP32, 1 = BF16, 2 = FP16 with a power-of-two max-abs scale per
+ * 32x16 block of each plane); the forward scatters from the image buffer
+ * into the receiver buffer with the same stored values, recomputing the
+ * source field; the adjoint images the receiver buffer into the image buffer.
+ * Forward and adjoint are exact transposes of each other (up to FP32
+ * rounding), unlike the reference's rtm_forward / rtm_adjoint pair. */
+int sepx_lin_source_pass(int jt, int npts, int nt, int js, int prec);
+int sepx_lin_forward_resident(int jt, int npts, int nt, int js, int prec);
+int sepx_lin_adjoint_resident(int jt, int nt, int js, int prec);
+long long sepx_snapshot_bytes(int nt, int js, int prec);
 int sepx_set_image(const float *img);                 /* host, dense */
 int sepx_get_image(float *img);                       /* host, dense */
 int sepx_set_source_fields(const float *p0, const float *p1);
@@ -99,6 +111,11 @@ int sepx_get_traces(float *vals);
 int sepx_zero_traces(void);                          /* receiver buffer := 0 on the device */
 int sepx_synchronize(void);
 void *sepx_get_stream(void);          /* the cudaStream_t every call enqueues on */
+
+/* FP64-accumulated dot product of two device float vectors (b == NULL: the
+ * sum of a), as my_vector::dot (Born/hypercube_float.cpp:123-133); the result
+ * is written to host memory; synchronous. */
+int sepx_dot_f32(const float *a, const float *b, long long n, double *result);
 
 /* Diagnostics and tuning. */
 const char *sepx_last_error(void);

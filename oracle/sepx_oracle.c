@@ -373,6 +373,81 @@ void orc_map_data_adjoint(int add, int ntb, int nt, int n2, int n3, float *m, co
 }
 
 /* ------------------------------------------------------------------------ */
+/* Snapshot quantisation of the product's linearised operator (test mirror):
+ * blocks of 32 x 16 cells of each plane of the updated interior, tiles
+ * anchored at x = y = 4; scale = 2^(e-15) with max|u| < 2^e (frexp), values
+ * u/scale rounded to BF16 or FP16 (round to nearest even) and multiplied
+ * back.  prec 0 keeps the values. */
+static float bf16_round(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;   /* inf / nan */
+  uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7fffu + lsb;
+  u &= 0xffff0000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+
+static float f16_round(float x) {
+  /* nearest-even binary16 value of x, returned as float (|x| < 2^15 here) */
+  const float a = fabsf(x);
+  if (a == 0.0f || a != a) return x;
+  int e;
+  frexpf(a, &e);                          /* a in [2^(e-1), 2^e) */
+  int q = e - 1 - 10;                     /* spacing exponent of 11-bit significands */
+  if (q < -24) q = -24;                   /* subnormal spacing 2^-24 */
+  const float step = ldexpf(1.0f, q);
+  const float r = nearbyintf(a / step) * step;   /* a/step exact: power-of-two division */
+  return x < 0 ? -r : r;
+}
+
+static void snap_quantise_blocks(const orc_grid *g, void *vol, int prec, int is_double) {
+  if (prec == 0) return;
+  const int n1 = g->n1, n2 = g->n2, n3 = g->n3;
+  const long n12 = (long)n1 * n2;
+  const int xe = 4 + 16 * ((n1 - 8) / 16), ye = 4 + 16 * ((n2 - 8) / 16), ze = n3 - 8;
+#pragma omp parallel for schedule(static)
+  for (int z = 4; z < ze; z++)
+    for (int y0 = 4; y0 < ye; y0 += 16)
+      for (int x0 = 4; x0 < xe; x0 += 32) {
+        const int x1 = x0 + 32 < xe ? x0 + 32 : xe;
+        float mx = 0.f;
+        for (int y = y0; y < y0 + 16; y++)
+          for (int x = x0; x < x1; x++) {
+            const long i = z * n12 + (long)y * n1 + x;
+            const float v = is_double ? (float)((double *)vol)[i] : ((float *)vol)[i];
+            if (fabsf(v) > mx) mx = fabsf(v);
+          }
+        float sc = 1.f, inv = 1.f;
+        if (mx > 0.f) {
+          int e;
+          frexpf(mx, &e);
+          if (e < -100) e = -100;
+          sc = ldexpf(1.0f, e - 15);
+          inv = ldexpf(1.0f, 15 - e);
+        }
+        for (int y = y0; y < y0 + 16; y++)
+          for (int x = x0; x < x1; x++) {
+            const long i = z * n12 + (long)y * n1 + x;
+            float v = is_double ? (float)((double *)vol)[i] : ((float *)vol)[i];
+            float w = v * inv;
+            w = (prec == 1) ? bf16_round(w) : f16_round(w);
+            w = w * sc;
+            if (is_double) ((double *)vol)[i] = w; else ((float *)vol)[i] = w;
+          }
+      }
+}
+
+static void snap_quantise_f32(const orc_ctx *b, float *vol, int prec) {
+  snap_quantise_blocks(&b->g, vol, prec, 0);
+}
+static void snap_quantise_f64(const orc_ctx *b, double *vol, int prec) {
+  snap_quantise_blocks(&b->g, vol, prec, 1);
+}
+
+/* ------------------------------------------------------------------------ */
 /* precision-generic kernels and loops */
 #define REAL float
 #define FMA fmaf
@@ -453,6 +528,31 @@ int orc_rtm_adjoint_f32(const orc_ctx *c, const float *vel, int jt, const float 
 static void fill64(const orc_ctx64 *c, ctx64_full *f) {
   f->c = c;
   fd_coeffs_d(c->d1, c->d2, c->d3, f->coef);
+}
+
+int orc_lin_source_f32(const orc_ctx *c, const float *vel, int jt, int npts, int nt, int js,
+                       int prec, float *snaps) {
+  return lin_source_impl_f32(c, vel, jt, npts, nt, js, prec, snaps);
+}
+int orc_lin_forward_f32(const orc_ctx *c, const float *vel, int jt, int npts, int nt, int js,
+                        int prec, const float *m, float *dat) {
+  return lin_forward_impl_f32(c, vel, jt, npts, nt, js, prec, m, dat);
+}
+int orc_lin_adjoint_f32(const orc_ctx *c, const float *vel, int jt, int nt, int js,
+                        const float *snaps, const float *dat, float *img) {
+  return lin_adjoint_impl_f32(c, vel, jt, nt, js, snaps, dat, img);
+}
+int orc_lin_source_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt, int js,
+                       double *snaps) {
+  ctx64_full f;
+  fill64(c, &f);
+  return lin_source_impl_f64(&f, vel, jt, npts, nt, js, 0, snaps);
+}
+int orc_lin_adjoint_f64(const orc_ctx64 *c, const double *vel, int jt, int nt, int js,
+                        const double *snaps, const double *dat, double *img) {
+  ctx64_full f;
+  fill64(c, &f);
+  return lin_adjoint_impl_f64(&f, vel, jt, nt, js, snaps, dat, img);
 }
 
 int orc_source_prop_f64(const orc_ctx64 *c, const double *vel, double *p0_out, double *p1_out,

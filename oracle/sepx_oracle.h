@@ -122,6 +122,19 @@ int orc_rtm_forward_f64(const orc_ctx64 *c, const double *vel, int jt, const dou
 int orc_rtm_adjoint_f64(const orc_ctx64 *c, const double *vel, int jt, const double *p0_s,
                         const double *p1_s, double *img, const double *dat, int npts_src, int nt);
 
+/* linearised Born pair with quantised source snapshots (prec 0 FP32, 1 BF16,
+ * 2 FP16); snaps holds ceil(nt/js) full volumes */
+int orc_lin_source_f32(const orc_ctx *c, const float *vel, int jt, int npts, int nt, int js,
+                       int prec, float *snaps);
+int orc_lin_forward_f32(const orc_ctx *c, const float *vel, int jt, int npts, int nt, int js,
+                        int prec, const float *m, float *dat);
+int orc_lin_adjoint_f32(const orc_ctx *c, const float *vel, int jt, int nt, int js,
+                        const float *snaps, const float *dat, float *img);
+int orc_lin_source_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt, int js,
+                       double *snaps);
+int orc_lin_adjoint_f64(const orc_ctx64 *c, const double *vel, int jt, int nt, int js,
+                        const double *snaps, const double *dat, double *img);
+
 /* threads used by the OpenMP loops */
 int orc_num_threads(void);
 void orc_set_num_threads(int n);

@@ -22,6 +22,7 @@
 
 #include "../../include/sepx.h"
 #include "sepx_aux.h"
+#include "sepx_blas.h"
 #include "sepx_device.cuh"
 #include "sepx_prop.h"
 
@@ -88,6 +89,14 @@ struct Ctx {
   size_t inj_cap = 0;
   float *d_stage = nullptr;
   size_t stage_cap = 0;
+  double *d_dot = nullptr;    // dot-product partials + result
+  size_t dot_cap = 0;
+  // compressed source snapshots of the linearised pair
+  unsigned char *d_snap = nullptr;
+  size_t snap_cap = 0;
+  float *d_snap_scale = nullptr;
+  size_t snap_scale_cap = 0;
+  int snap_js = 0, snap_prec = -1, snap_nt = -1;
 };
 
 Ctx G;
@@ -431,6 +440,127 @@ int loop_rtm_adjoint(int jt, int npts, int nt) {
   return 0;
 }
 
+// ---------------------------------------------------------- linearised Born pair
+long long snap_blocks_per_step() {
+  const PropGeom &g = G.geom;
+  const long long ntx = (g.xe - g.xb + kTX - 1) / kTX, nty = (g.ye - g.yb) / kTY;
+  return ntx * nty * std::max(0, g.ze - g.zb);
+}
+
+int ensure_snapshots(int nt, int js, int prec) {
+  if (js < 1) return fail("snapshot interval must be >= 1");
+  if (prec < kSnapF32 || prec > kSnapF16) return fail("unknown snapshot precision %d", prec);
+  const long long nsnap = (nt + js - 1) / js;
+  const long long blocks = snap_blocks_per_step() * std::max(1LL, nsnap);
+  const size_t bytes = (size_t)blocks * kCenterFloats * (prec == kSnapF32 ? 4 : 2);
+  RET(ensure(&G.d_snap, &G.snap_cap, bytes));
+  RET(ensure(&G.d_snap_scale, &G.snap_scale_cap, (size_t)blocks));
+  return 0;
+}
+
+PropParams lin_params(int js, int prec) {
+  PropParams P = base_params();
+  P.snap = G.d_snap;
+  P.snap_scale = G.d_snap_scale;
+  P.snap_prec = prec;
+  (void)js;
+  return P;
+}
+
+// source wavefield u_t, t = 0..nt-1, stored every js steps
+int loop_lin_source(int jt, int npts, int nt, int js, int prec) {
+  RET(need_grid());
+  if (!G.vel_set) return fail("transfer_vel_func1 must be called first");
+  if (jt < 1 || nt < 0) return fail("invalid jt=%d / nt=%d", jt, nt);
+  RET(ensure_snapshots(nt, js, prec));
+  RET(prep_inj(npts, jt, nt, 0, 1.0f));
+  Volume *A = &G.F[2], *B = &G.F[3];
+  RET(zero_volume(*A));
+  RET(zero_volume(*B));
+  PropParams P = lin_params(js, prec);
+  P.src.plane_slot = npts > 0 ? G.srcmap.plane_slot : nullptr;
+  P.src.map = G.srcmap.map;
+  P.src.next = G.srcmap.next;
+  for (int it = 0; it < nt; it++) {
+    set_field(P, 0, *B, *A);
+    P.inj_s = G.d_inj + (size_t)it * std::max(npts, 0);
+    P.do_snap = (it % js == 0);
+    P.snap_index = it / js;
+    CKL(launch_prop_step(kLinSrc, P, G.stream));
+    std::swap(A, B);
+  }
+  G.snap_js = js;
+  G.snap_prec = prec;
+  G.snap_nt = nt;
+  return 0;
+}
+
+// traces += R v_t with v from the model in the image buffer
+int loop_lin_forward(int jt, int npts, int nt, int js, int prec) {
+  RET(need_grid());
+  if (!G.vel_set) return fail("transfer_vel_func1 must be called first");
+  if (jt < 1 || nt < 0) return fail("invalid jt=%d / nt=%d", jt, nt);
+  RET(prep_receivers(jt, nt));
+  RET(prep_inj(npts, jt, nt, 0, 1.0f));
+  if (prec < kSnapF32 || prec > kSnapF16 || js < 1) return fail("invalid snapshot settings");
+  Volume *D0 = &G.F[0], *D1 = &G.F[1], *S0 = &G.F[2], *S1 = &G.F[3];
+  for (auto *v : {D0, D1, S0, S1}) RET(zero_volume(*v));
+  PropParams P = lin_params(js, prec);
+  P.src.plane_slot = npts > 0 ? G.srcmap.plane_slot : nullptr;
+  P.src.map = G.srcmap.map;
+  P.src.next = G.srcmap.next;
+  P.rec.plane_slot = G.recmap.plane_slot;
+  P.rec.map = G.recmap.map;
+  P.rec.next = G.recmap.next;
+  P.trc = G.d_trc;
+  P.nrec = G.rec_nx * G.rec_ny;
+  for (int it = 0; it < nt; it++) {
+    const int id = it / jt, ii = it - id * jt;
+    set_field(P, 0, *D1, *D0);
+    set_field(P, 1, *S1, *S0);
+    P.inj_s = G.d_inj + (size_t)it * std::max(npts, 0);
+    P.do_snap = P.do_scatter = (it % js == 0);
+    P.snap_index = it / js;
+    P.trc_id = id;
+    P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
+    CKL(launch_prop_step(kLinFwd, P, G.stream));
+    std::swap(D0, D1);
+    std::swap(S0, S1);
+  }
+  return 0;
+}
+
+// image := sum_t c u^_t w_t with w from the traces (the exact transpose)
+int loop_lin_adjoint(int jt, int nt, int js, int prec) {
+  RET(need_grid());
+  if (!G.vel_set) return fail("transfer_vel_func1 must be called first");
+  if (jt < 1 || nt < 0) return fail("invalid jt=%d / nt=%d", jt, nt);
+  if (G.snap_nt != nt || G.snap_js != js || G.snap_prec != prec)
+    return fail("no source snapshots for nt=%d js=%d prec=%d: run the source pass first", nt, js, prec);
+  RET(prep_receivers(jt, nt));
+  Volume *D0 = &G.F[0], *D1 = &G.F[1];
+  RET(zero_volume(*D0));
+  RET(zero_volume(*D1));
+  RET(zero_volume(G.img));
+  PropParams P = lin_params(js, prec);
+  P.rec.plane_slot = G.recmap.plane_slot;
+  P.rec.map = G.recmap.map;
+  P.rec.next = G.recmap.next;
+  P.trc = G.d_trc;
+  P.nrec = G.rec_nx * G.rec_ny;
+  for (int it = nt - 1; it >= 0; it--) {
+    const int id = it / jt, ii = it - id * jt;
+    set_field(P, 0, *D1, *D0);
+    P.do_snap = P.do_image = (it % js == 0);
+    P.snap_index = it / js;
+    P.trc_id = id;
+    P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
+    CKL(launch_prop_step(kLinAdj, P, G.stream));
+    std::swap(D0, D1);
+  }
+  return 0;
+}
+
 // traces: host trace-major [nrec][nt] <-> device time-major [nt][nrec]
 int traces_h2d(const float *vals, int nrec, int nt) {
   const size_t chunk = std::max<size_t>(1, (size_t)(64u << 20) / std::max(nt, 1));
@@ -668,6 +798,25 @@ int sepx_rtm_adjoint_resident(int jt, int npts, int nt, int use_source_last) {
   return loop_rtm_adjoint(jt, npts, nt);
 }
 
+int sepx_lin_source_pass(int jt, int npts, int nt, int js, int prec) {
+  return loop_lin_source(jt, npts, nt, js, prec);
+}
+
+int sepx_lin_forward_resident(int jt, int npts, int nt, int js, int prec) {
+  return loop_lin_forward(jt, npts, nt, js, prec);
+}
+
+int sepx_lin_adjoint_resident(int jt, int nt, int js, int prec) {
+  return loop_lin_adjoint(jt, nt, js, prec);
+}
+
+long long sepx_snapshot_bytes(int nt, int js, int prec) {
+  if (!G.have_grid || js < 1) return -1;
+  const long long nsnap = (nt + js - 1) / js;
+  return snap_blocks_per_step() * std::max(1LL, nsnap) * kCenterFloats * (prec == kSnapF32 ? 4 : 2) +
+         snap_blocks_per_step() * std::max(1LL, nsnap) * 4;
+}
+
 int sepx_set_image(const float *img) {
   RET(need_grid());
   RET(h2d_volume(G.img, img));
@@ -715,6 +864,17 @@ int sepx_get_traces(float *vals) {
 int sepx_zero_traces(void) {
   RET(need_grid());
   if (G.d_trc && G.trc_cap) CK(cudaMemsetAsync(G.d_trc, 0, G.trc_cap * sizeof(float), G.stream));
+  return 0;
+}
+
+int sepx_dot_f32(const float *a, const float *b, long long n, double *result) {
+  RET(need_device());
+  if (n < 0 || !result) return fail("sepx_dot_f32: invalid arguments");
+  const int np = vec_dot_scratch_doubles();
+  RET(ensure(&G.d_dot, &G.dot_cap, (size_t)np + 1));
+  CKL(vec_dot(a, b, n, G.d_dot, G.d_dot + np, G.stream));
+  CK(cudaMemcpyAsync(result, G.d_dot + np, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+  CK(cudaStreamSynchronize(G.stream));
   return 0;
 }
 

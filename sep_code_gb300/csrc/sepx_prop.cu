@@ -27,6 +27,8 @@
 // __fmaf_rn / __fmul_rn / __fadd_rn, no contraction freedom), so a step is
 // bit-identical to the CPU restatement.
 #include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "sepx_device.cuh"
@@ -36,19 +38,26 @@ namespace sepx {
 
 template <int MODE>
 struct Mode {
-  static constexpr int NF = (MODE == kBornFwd || MODE == kRtmAdj) ? 2 : 1;
-  static constexpr bool F0_VEL_INSIDE = (MODE == kBornFwd);   // wave_kernel_adj
+  static constexpr bool LIN = (MODE == kLinSrc || MODE == kLinFwd || MODE == kLinAdj);
+  static constexpr int NF = (MODE == kBornFwd || MODE == kRtmAdj || MODE == kLinFwd) ? 2 : 1;
+  static constexpr bool F0_VEL_INSIDE = (MODE == kBornFwd || MODE == kLinFwd);  // wave_kernel_adj
   static constexpr bool VEL_HALO = F0_VEL_INSIDE;
-  static constexpr bool HAS_IMG = (MODE != kSrcProp);
+  static constexpr bool HAS_IMG = (MODE != kSrcProp && MODE != kLinSrc);
   static constexpr bool HAS_AUX = (MODE == kRtmAdj1);
-  // sponge passes per step on each field (write-time multiplies, extra
-  // multiplies of the previous field)
-  static constexpr int KW0 = (MODE == kBornFwd) ? 2 : ((MODE == kSrcProp) ? 0 : 1);
+  // sponge passes per step: KW* multiplies at write time, KP* extra multiplies
+  // of the previous field; PRE0: field 0 is damped once before the epilogue
+  // (kLinFwd: v = T (L(Vv) + 2v - T v_prev) + scattering)
+  static constexpr int KW0 = (MODE == kBornFwd) ? 2
+                             : ((MODE == kSrcProp || MODE == kLinSrc || MODE == kLinFwd) ? 0 : 1);
+  static constexpr int KP0 = (MODE == kLinFwd) ? 1 : KW0;
+  static constexpr bool PRE0 = (MODE == kLinFwd);
   static constexpr int KW1 = (MODE == kBornFwd) ? 1 : 0;
-  static constexpr bool SRC_INJ = (MODE == kSrcProp || MODE == kBornFwd);
-  static constexpr int SRC_FIELD = (MODE == kSrcProp) ? 0 : 1;
-  static constexpr bool REC_EXTRACT = (MODE == kBornFwd);
-  static constexpr bool REC_INJECT = (MODE == kRtmAdj || MODE == kRtmAdj1);
+  static constexpr bool NEED_T = (KW0 > 0 || KP0 > 0 || KW1 > 0 || PRE0);
+  static constexpr bool SRC_INJ = (MODE == kSrcProp || MODE == kBornFwd || MODE == kLinSrc ||
+                                   MODE == kLinFwd);
+  static constexpr int SRC_FIELD = (MODE == kSrcProp || MODE == kLinSrc) ? 0 : 1;
+  static constexpr bool REC_EXTRACT = (MODE == kBornFwd || MODE == kLinFwd);
+  static constexpr bool REC_INJECT = (MODE == kRtmAdj || MODE == kRtmAdj1 || MODE == kLinAdj);
   // stage layout (floats)
   static constexpr int FEED = 0;
   static constexpr int FEEDV = FEED + NF * kCenterFloats;
@@ -64,6 +73,40 @@ struct Mode {
             (HAS_AUX ? kCenterFloats : 0));
   static constexpr uint32_t BYTES_IMG = BYTES_NOIMG + (HAS_IMG ? 4u * kCenterFloats : 0u);
 };
+
+// ---- compressed snapshots: power-of-two max-abs scale per 32x16 block-plane ----
+// sc = 2^(e-15) with blockmax < 2^e, so |u/sc| < 2^15: the scaling is exact and
+// FP16 keeps small values normal down to 2^-29 of the block maximum.
+__device__ __forceinline__ float snap_scale_of(float bmax, int prec) {
+  if (prec == kSnapF32 || !(bmax > 0.f)) return 1.0f;
+  int e;
+  frexpf(bmax, &e);
+  e = max(e, -100);
+  return ldexpf(1.0f, e - 15);
+}
+
+__device__ __forceinline__ unsigned short snap_q(float u, float inv, int prec) {
+  const float x = __fmul_rn(u, inv);
+  if (prec == kSnapBF16) return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+  return __half_as_ushort(__float2half_rn(x));
+}
+
+__device__ __forceinline__ float snap_dq(unsigned short q, float sc, int prec) {
+  const float x = (prec == kSnapBF16) ? __bfloat162float(__ushort_as_bfloat16(q))
+                                      : __half2float(__ushort_as_half(q));
+  return __fmul_rn(x, sc);
+}
+
+// max over the 128 consumer threads (named barrier 1); every consumer calls it
+__device__ __forceinline__ float consumer_max(float m, float *red, int warp, int lane) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) red[warp] = m;
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+  const float r = fmaxf(fmaxf(red[0], red[1]), fmaxf(red[2], red[3]));
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+  return r;
+}
 
 // Sponge factor of damp_kernel (Born/wave_fkernel.3d8o.cu:183-210), one GPU:
 // cells with x < xg, y < yg and edge = distance to the nearest face minus 4
@@ -159,6 +202,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
                                           ~static_cast<uintptr_t>(127));
   unsigned long long *bar_full = reinterpret_cast<unsigned long long *>(smem + STAGES * M::STAGE);
   unsigned long long *bar_empty = bar_full + STAGES;
+  float *red = reinterpret_cast<float *>(bar_empty + STAGES);   // 4 floats: block max
 
   const PropGeom &g = P.g;
   const int tid = threadIdx.x;
@@ -178,7 +222,8 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
   }
   __syncthreads();
 
-  const bool load_img = M::HAS_IMG && (MODE == kBornFwd ? P.do_scatter : P.do_image);
+  const bool load_img =
+      M::HAS_IMG && ((MODE == kBornFwd || MODE == kLinFwd) ? P.do_scatter : P.do_image);
   const uint32_t stage_bytes = load_img ? M::BYTES_IMG : M::BYTES_NOIMG;
   int issued = 0;
 
@@ -291,23 +336,26 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&bar_empty[s]));
 
+      float t[4] = {1.f, 1.f, 1.f, 1.f};
+      float val[NF][4];
+      const long long cell = rowoff + g.plane * z;
       if (active) {
-        float t[4];
+        if (M::NEED_T) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) t[c] = (M::KW0 > 0 || M::KW1 > 0) ? sponge(P, x + c, y, z) : 1.f;
-        float val[NF][4];
+          for (int c = 0; c < 4; c++) t[c] = sponge(P, x + c, y, z);
+        }
 #pragma unroll
         for (int f = 0; f < NF; f++) {
-          const int kp = (f == 0) ? M::KW0 : M::KW1;
+          const int kp = (f == 0) ? M::KP0 : M::KW1;
 #pragma unroll
           for (int c = 0; c < 4; c++) {
             float pv = comp(prevv[f], c);
             if (kp == 1) pv = damp_k<1>(pv, t[c]);
             if (kp == 2) pv = damp_k<2>(pv, t[c]);
             val[f][c] = __fsub_rn(res[f][c], pv);
+            if (f == 0 && M::PRE0) val[f][c] = __fmul_rn(val[f][c], t[c]);
           }
         }
-        const long long cell = rowoff + g.plane * z;
         // source injection into the new field (ids in ascending order)
         if (M::SRC_INJ && P.src.plane_slot) {
           const int slot = __ldg(P.src.plane_slot + z);
@@ -338,14 +386,61 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
             }
           }
         }
+      }
+
+      // snapshot block: scale from the block maximum of the new source field
+      // (stored by kLinSrc, recomputed identically by kLinFwd)
+      float sc = 1.f;
+      long long blk = 0, eoff = 0;
+      if (M::LIN) {
+        const int ntx = (g.xe - g.xb + kTX - 1) / kTX, nty = (g.ye - g.yb) / kTY;
+        blk = ((P.snap_index * (g.ze - g.zb) + (z - g.zb)) * nty + blockIdx.y) * ntx + blockIdx.x;
+        eoff = blk * kCenterFloats + row * kTX + 4 * xq;
+      }
+      if ((MODE == kLinSrc || MODE == kLinFwd) && P.do_snap && P.snap_prec != kSnapF32) {
+        constexpr int sf = (MODE == kLinSrc) ? 0 : (NF - 1);
+        float m = 0.f;
+        if (active) {
+#pragma unroll
+          for (int c = 0; c < 4; c++) m = fmaxf(m, fabsf(val[sf][c]));
+        }
+        sc = snap_scale_of(consumer_max(m, red, warp, lane), P.snap_prec);
+      }
+
+      if (active) {
         const float s6 = (float)0.000001;
-        if (MODE == kBornFwd) {
-          // Born scattering: rec += 1e-6 src img over x < xg, y < yg
+        if (MODE == kLinSrc && P.do_snap) {
+          if (tid == 0) P.snap_scale[blk] = sc;
+          if (P.snap_prec == kSnapF32) {
+            *reinterpret_cast<float4 *>(reinterpret_cast<float *>(P.snap) + eoff) =
+                make_float4(val[0][0], val[0][1], val[0][2], val[0][3]);
+          } else {
+            const float inv = __fdiv_rn(1.0f, sc);
+            uint2 pk;
+            pk.x = (uint32_t)snap_q(val[0][0], inv, P.snap_prec) |
+                   ((uint32_t)snap_q(val[0][1], inv, P.snap_prec) << 16);
+            pk.y = (uint32_t)snap_q(val[0][2], inv, P.snap_prec) |
+                   ((uint32_t)snap_q(val[0][3], inv, P.snap_prec) << 16);
+            *reinterpret_cast<uint2 *>(reinterpret_cast<unsigned short *>(P.snap) + eoff) = pk;
+          }
+        }
+        if (MODE == kBornFwd || MODE == kLinFwd) {
+          // Born scattering: rec += 1e-6 src img over x < xg, y < yg (kLinFwd:
+          // with the snapshot value of the source field)
           if (P.do_scatter && y < g.yg) {
+            float u[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) u[c] = val[NF - 1][c];
+            if (MODE == kLinFwd && P.snap_prec != kSnapF32) {
+              const float inv = __fdiv_rn(1.0f, sc);
+#pragma unroll
+              for (int c = 0; c < 4; c++)
+                u[c] = snap_dq(snap_q(u[c], inv, P.snap_prec), sc, P.snap_prec);
+            }
 #pragma unroll
             for (int c = 0; c < 4; c++)
               if (x + c < g.xg)
-                val[0][c] = __fmaf_rn(__fmul_rn(s6, val[1][c]), comp(imgv, c), val[0][c]);
+                val[0][c] = __fmaf_rn(__fmul_rn(s6, u[c]), comp(imgv, c), val[0][c]);
           }
           // receiver extraction from the new scattered field
           const int slot = P.rec.plane_slot ? __ldg(P.rec.plane_slot + z) : -1;
@@ -364,10 +459,24 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
             }
           }
         }
-        if (MODE == kRtmAdj || MODE == kRtmAdj1) {
+        if (MODE == kRtmAdj || MODE == kRtmAdj1 || MODE == kLinAdj) {
           if (P.do_image && y < g.yg) {
-            float4 src = (MODE == kRtmAdj) ? make_float4(val[1][0], val[1][1], val[1][2], val[1][3])
-                                           : auxv;
+            float4 src;
+            if (MODE == kRtmAdj) {
+              src = make_float4(val[1][0], val[1][1], val[1][2], val[1][3]);
+            } else if (MODE == kRtmAdj1) {
+              src = auxv;
+            } else if (P.snap_prec == kSnapF32) {
+              src = ldg4(reinterpret_cast<const float *>(P.snap) + eoff);
+            } else {
+              const float bsc = __ldg(P.snap_scale + blk);
+              const uint2 pk =
+                  __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const unsigned short *>(P.snap) + eoff));
+              src = make_float4(snap_dq((unsigned short)(pk.x & 0xffffu), bsc, P.snap_prec),
+                                snap_dq((unsigned short)(pk.x >> 16), bsc, P.snap_prec),
+                                snap_dq((unsigned short)(pk.y & 0xffffu), bsc, P.snap_prec),
+                                snap_dq((unsigned short)(pk.y >> 16), bsc, P.snap_prec));
+            }
             float o[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
@@ -413,7 +522,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
 
 template <int MODE, int STAGES>
 constexpr size_t smem_bytes_of() {
-  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 128;
+  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 16 + 128;
 }
 
 template <int MODE, int STAGES>
@@ -441,6 +550,9 @@ cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
     case kBornFwd: return launch_mode<kBornFwd, 3>(P, grid, st);
     case kRtmAdj: return launch_mode<kRtmAdj, 3>(P, grid, st);
     case kRtmAdj1: return launch_mode<kRtmAdj1, 3>(P, grid, st);
+    case kLinSrc: return launch_mode<kLinSrc, 4>(P, grid, st);
+    case kLinFwd: return launch_mode<kLinFwd, 3>(P, grid, st);
+    case kLinAdj: return launch_mode<kLinAdj, 3>(P, grid, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -451,6 +563,9 @@ size_t prop_smem_bytes(int mode) {
     case kBornFwd: return smem_bytes_of<kBornFwd, 3>();
     case kRtmAdj: return smem_bytes_of<kRtmAdj, 3>();
     case kRtmAdj1: return smem_bytes_of<kRtmAdj1, 3>();
+    case kLinSrc: return smem_bytes_of<kLinSrc, 4>();
+    case kLinFwd: return smem_bytes_of<kLinFwd, 3>();
+    case kLinAdj: return smem_bytes_of<kLinAdj, 3>();
   }
   return 0;
 }

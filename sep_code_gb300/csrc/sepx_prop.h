@@ -27,7 +27,20 @@ constexpr int kThreads = kConsumerThreads + 32;            // + one TMA producer
 //            rebuilt backwards (no sponge), receiver injection, imaging
 //  kRtmAdj1  first rtm_adjoint step: receiver field only, imaging against the
 //            given last source wavefield
-enum PropMode : int { kSrcProp = 0, kBornFwd = 1, kRtmAdj = 2, kRtmAdj1 = 3 };
+//  kLinSrc   source pass of the linearised Born pair: as kSrcProp, and on
+//            snapshot steps the new field is stored compressed
+//  kLinFwd   linearised Born forward: scattered field v_t = T (L(V v) + 2v)
+//            - T^2 v_{t-2} + c u^_t m (u^ = the stored snapshot value,
+//            recomputed bit-identically from the source field carried along),
+//            receiver extraction; the exact transpose of kLinAdj
+//  kLinAdj   linearised adjoint: receiver field as kRtmAdj's, imaging
+//            against the stored snapshots
+enum PropMode : int {
+  kSrcProp = 0, kBornFwd = 1, kRtmAdj = 2, kRtmAdj1 = 3, kLinSrc = 4, kLinFwd = 5, kLinAdj = 6
+};
+
+// snapshot storage of the source wavefield
+enum SnapPrec : int { kSnapF32 = 0, kSnapBF16 = 1, kSnapF16 = 2 };
 
 // Cells that carry sources or receivers, indexed by z plane so the kernel
 // tests a single flag per plane.
@@ -71,6 +84,13 @@ struct alignas(64) PropParams {
   const float *sinc_row;      // 8 receiver interpolation taps of this step
   int do_scatter;             // Born scattering this step (it % jt == 0)
   int do_image;               // imaging this step (it % jt == 0)
+  // snapshots (kLin*): block (32 x 16 cells of one plane) b of snapshot k is
+  // at element ((k*nzi + z-zb)*ntiles + b)*512; one float scale per block
+  int do_snap;                // store (kLinSrc) / use (kLinFwd, kLinAdj) this step
+  int snap_prec;              // SnapPrec
+  long long snap_index;       // k
+  void *snap;                 // storage
+  float *snap_scale;          // per-block scale (power of two)
   int *err;                   // device error word
 };
 
