@@ -91,6 +91,18 @@ class Oracle:
                                           C.c_int]
         L.orc_rtm_adjoint_f64.argtypes = [C.POINTER(OrcCtx64), F64P, C.c_int, F64P, F64P, F64P,
                                           F64P, C.c_int, C.c_int]
+        L.orc_lin_source_f32.argtypes = [C.POINTER(OrcCtx), F32P, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_int, F32P]
+        L.orc_lin_forward_f32.argtypes = [C.POINTER(OrcCtx), F32P, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, F32P, F32P]
+        L.orc_lin_adjoint_f32.argtypes = [C.POINTER(OrcCtx), F32P, C.c_int, C.c_int, C.c_int, F32P,
+                                          F32P, F32P]
+        L.orc_lin_source_f64.argtypes = [C.POINTER(OrcCtx64), F64P, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, F64P]
+        L.orc_lin_adjoint_f64.argtypes = [C.POINTER(OrcCtx64), F64P, C.c_int, C.c_int, C.c_int,
+                                          F64P, F64P, F64P]
+        L.orc_lin_forward_f64.argtypes = [C.POINTER(OrcCtx64), F64P, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, F64P, F64P]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
 

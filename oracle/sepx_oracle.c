@@ -548,6 +548,12 @@ int orc_lin_source_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, 
   fill64(c, &f);
   return lin_source_impl_f64(&f, vel, jt, npts, nt, js, 0, snaps);
 }
+int orc_lin_forward_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt, int js,
+                        const double *m, double *dat) {
+  ctx64_full f;
+  fill64(c, &f);
+  return lin_forward_impl_f64(&f, vel, jt, npts, nt, js, 0, m, dat);
+}
 int orc_lin_adjoint_f64(const orc_ctx64 *c, const double *vel, int jt, int nt, int js,
                         const double *snaps, const double *dat, double *img) {
   ctx64_full f;

@@ -132,6 +132,8 @@ int orc_lin_adjoint_f32(const orc_ctx *c, const float *vel, int jt, int nt, int 
                         const float *snaps, const float *dat, float *img);
 int orc_lin_source_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt, int js,
                        double *snaps);
+int orc_lin_forward_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt, int js,
+                        const double *m, double *dat);
 int orc_lin_adjoint_f64(const orc_ctx64 *c, const double *vel, int jt, int nt, int js,
                         const double *snaps, const double *dat, double *img);
 

@@ -53,6 +53,9 @@ def _load() -> C.CDLL:
         "sepx_device_error": [],
         "sepx_set_zchunk": [i],
         "sepx_reset": [],
+        "sepx_lin_source_pass": [i, i, i, i, i],
+        "sepx_lin_forward_resident": [i, i, i, i, i],
+        "sepx_lin_adjoint_resident": [i, i, i, i],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -61,6 +64,10 @@ def _load() -> C.CDLL:
     L.sepx_last_error.restype = C.c_char_p
     L.sepx_kernel_launches.restype = C.c_longlong
     L.sepx_get_stream.restype = C.c_void_p
+    L.sepx_snapshot_bytes.argtypes = [i, i, i]
+    L.sepx_snapshot_bytes.restype = C.c_longlong
+    L.sepx_dot_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_double)]
+    L.sepx_dot_f32.restype = C.c_int
     # host set-up math
     L.sepx_host_sinc_table.argtypes = [i, i, F32P]
     L.sepx_host_glibc_rand_sequence.argtypes = [C.c_uint, i, I32P]

@@ -23,6 +23,7 @@
 #include "../../include/sepx.h"
 #include "sepx_aux.h"
 #include "sepx_blas.h"
+#include "sepx_common.h"
 #include "sepx_device.cuh"
 #include "sepx_prop.h"
 
@@ -587,6 +588,17 @@ int traces_d2h(float *vals, int nrec, int nt) {
 }
 
 }  // namespace
+
+int set_error(const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  G.err = buf;
+  return -1;
+}
+
 }  // namespace sepx
 
 using namespace sepx;

@@ -97,6 +97,52 @@ def rtm_adjoint(p0_s, p1_s, jt, npts, nt):
     return img
 
 
+# ---------------------------------------------------------------- linearised pair
+SNAP_PREC = {"f32": 0, "bf16": 1, "f16": 2}
+
+
+def set_image(img) -> None:
+    check(lib.sepx_set_image(_f32(img)), "set_image")
+
+
+def get_image(shape):
+    out = np.zeros(shape, np.float32)
+    check(lib.sepx_get_image(out), "get_image")
+    return out
+
+
+def set_traces(vals) -> None:
+    check(lib.sepx_set_traces(_f32(vals)), "set_traces")
+
+
+def zero_traces() -> None:
+    check(lib.sepx_zero_traces(), "zero_traces")
+
+
+def get_traces(nrec, ntrace):
+    out = np.zeros((nrec, ntrace), np.float32)
+    check(lib.sepx_get_traces(out), "get_traces")
+    return out
+
+
+def lin_source_pass(jt, npts, nt, js=1, prec="f32") -> None:
+    check(lib.sepx_lin_source_pass(jt, npts, nt, js, SNAP_PREC[prec]), "lin_source_pass")
+
+
+def lin_forward(jt, npts, nt, js=1, prec="f32") -> None:
+    """traces (device receiver buffer) += L m, m = the image buffer"""
+    check(lib.sepx_lin_forward_resident(jt, npts, nt, js, SNAP_PREC[prec]), "lin_forward")
+
+
+def lin_adjoint(jt, nt, js=1, prec="f32") -> None:
+    """image buffer := L' d, d = the device receiver buffer"""
+    check(lib.sepx_lin_adjoint_resident(jt, nt, js, SNAP_PREC[prec]), "lin_adjoint")
+
+
+def snapshot_bytes(nt, js, prec) -> int:
+    return int(lib.sepx_snapshot_bytes(nt, js, SNAP_PREC[prec]))
+
+
 def synchronize() -> None:
     check(lib.sepx_synchronize(), "synchronize")
 

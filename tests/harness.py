@@ -100,3 +100,72 @@ class OracleShot:
         return self.orc.rtm_adjoint(ctx, st.vel2dt2, st.jtd, np.ascontiguousarray(p0_s, np.float32),
                                     np.ascontiguousarray(p1_s, np.float32),
                                     np.ascontiguousarray(traces, np.float32), 9, st.nt)
+
+
+PREC = {"f32": 0, "bf16": 1, "f16": 2}
+
+
+class LinCase:
+    """One shot of the linearised Born pair through the GPU and the oracle.
+    Model m lives on the padded grid (the image buffer); data d are receiver
+    traces [nrec][nt_big]."""
+
+    def __init__(self, s: M.Survey, st: M.ShotSetup):
+        self.s, self.st = s, st
+        _, self.vals = source_vals(s, st, 8)
+
+    # ---- GPU
+    def gpu_setup(self, traces=None):
+        st = self.st
+        g = GpuShot(self.s, st)
+        locs, _ = source_vals(self.s, st, 8)
+        gf.transfer_source_func(locs, self.vals)
+        gf.transfer_vel_func1(st.vel2dt2)
+        nrec = st.rnx * st.rny
+        tr = np.zeros((nrec, st.nt_big), np.float32) if traces is None else traces
+        gf.transfer_receiver_func(st.rnx, st.rny, st.rec_locs, tr)
+        return g
+
+    def gpu_forward(self, m, js, prec):
+        st = self.st
+        self.gpu_setup()
+        gf.set_image(m)
+        gf.zero_traces()
+        gf.lin_forward(st.jtd, 9, st.nt, js, prec)
+        return gf.get_traces(st.rnx * st.rny, st.nt_big)
+
+    def gpu_adjoint(self, d, js, prec, source_pass=True):
+        st = self.st
+        self.gpu_setup(traces=d)
+        if source_pass:
+            gf.lin_source_pass(st.jtd, 9, st.nt, js, prec)
+        gf.lin_adjoint(st.jtd, st.nt, js, prec)
+        return gf.get_image((st.n[2], st.n[1], st.n[0]))
+
+    # ---- oracle
+    def orc_ctx(self, orc):
+        return oracle_ctx(orc, self.s, self.st, self.vals)
+
+    def orc_forward(self, orc, m, js, prec):
+        import ctypes as C
+        st = self.st
+        ctx, keep = self.orc_ctx(orc)
+        dat = np.zeros((st.rnx * st.rny, st.nt_big), np.float32)
+        rc = orc.lib.orc_lin_forward_f32(C.byref(ctx), st.vel2dt2, st.jtd, 9, st.nt, js, PREC[prec],
+                                         np.ascontiguousarray(m, np.float32), dat)
+        assert rc == 0
+        return dat
+
+    def orc_adjoint(self, orc, d, js, prec):
+        import ctypes as C
+        st = self.st
+        ctx, keep = self.orc_ctx(orc)
+        nsnap = (st.nt + js - 1) // js
+        snaps = np.zeros((nsnap, st.n[2], st.n[1], st.n[0]), np.float32)
+        rc = orc.lib.orc_lin_source_f32(C.byref(ctx), st.vel2dt2, st.jtd, 9, st.nt, js, PREC[prec], snaps)
+        assert rc == 0
+        img = np.zeros((st.n[2], st.n[1], st.n[0]), np.float32)
+        rc = orc.lib.orc_lin_adjoint_f32(C.byref(ctx), st.vel2dt2, st.jtd, st.nt, js, snaps,
+                                         np.ascontiguousarray(d, np.float32), img)
+        assert rc == 0
+        return img

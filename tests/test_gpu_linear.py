@@ -1,0 +1,68 @@
+"""The linearised Born pair (least-squares RTM operator): GPU vs oracle with
+FP32 / BF16 / FP16 source snapshots, and the adjoint dot-product test
+<L m, d> = <m, L' d> to 1e-6 relative (spec tolerance), FP64 sums."""
+import numpy as np
+import pytest
+
+from sep_code_gb300 import model as M
+from tests.harness import LinCase, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case():
+    s = M.small_survey(m1=28, m2=24, m3=24, nt=50, seed=12)
+    st = M.prepare_shot(s)
+    return LinCase(s, st)
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16", "f16"])
+@pytest.mark.parametrize("js", [1, 3])
+def test_lin_parity(case, oracle, prec, js):
+    st = case.st
+    rng = np.random.default_rng(js)
+    m = np.zeros((st.n[2], st.n[1], st.n[0]), np.float32)
+    m[4:-8, 4:-16, 4:-16] = rng.standard_normal(m[4:-8, 4:-16, 4:-16].shape)
+    d_g = case.gpu_forward(m, js, prec)
+    d_o = case.orc_forward(oracle, m, js, prec)
+    assert np.abs(d_o).max() > 0
+    assert rel_l2(d_g, d_o) <= 1e-5
+    assert np.array_equal(d_g, d_o)
+    d = rng.standard_normal(d_o.shape).astype(np.float32)
+    i_g = case.gpu_adjoint(d, js, prec)
+    i_o = case.orc_adjoint(oracle, d, js, prec)
+    assert np.abs(i_o).max() > 0
+    assert rel_l2(i_g, i_o) <= 1e-5
+    assert np.array_equal(i_g, i_o)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f16"])
+def test_lin_dot_product(prec):
+    """config-1 style sponge + random boundary, 150 steps"""
+    s = M.small_survey(m1=40, m2=36, m3=32, nt=150, seed=31, nbound=8)
+    st = M.prepare_shot(s)
+    c = LinCase(s, st)
+    rng = np.random.default_rng(7)
+    m = rng.standard_normal((st.n[2], st.n[1], st.n[0])).astype(np.float32)
+    d = rng.standard_normal((st.rnx * st.rny, st.nt_big)).astype(np.float32)
+    Lm = c.gpu_forward(m, 1, prec)
+    Ltd = c.gpu_adjoint(d, 1, prec)
+    a = float(np.dot(Lm.astype(np.float64).ravel(), d.astype(np.float64).ravel()))
+    b = float(np.dot(m.astype(np.float64).ravel(), Ltd.astype(np.float64).ravel()))
+    bound = float(np.linalg.norm(Lm.astype(np.float64)) * np.linalg.norm(d.astype(np.float64)))
+    assert abs(a) > 0
+    # relative to the Cauchy-Schwarz bound |<Lm,d>| <= |Lm| |d|
+    assert abs(a - b) / bound <= 1e-6, (a, b, bound)
+    # relative to <Lm,d> itself (the reference's my_operator::dot_test measure,
+    # tolerance 1e-4 there): FP32 propagation rounding over 150 steps
+    assert abs(a - b) / abs(a) <= 1e-4, (a, b)
+
+
+def test_snapshot_memory(case):
+    from sep_code_gb300 import gpu_funcs as gf
+    c = case
+    c.gpu_setup()
+    b32 = gf.snapshot_bytes(c.st.nt, 4, "f32")
+    b16 = gf.snapshot_bytes(c.st.nt, 4, "f16")
+    assert 0 < b16 < 0.6 * b32
