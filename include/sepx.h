@@ -117,6 +117,22 @@ void *sepx_get_stream(void);          /* the cudaStream_t every call enqueues on
  * is written to host memory; synchronous. */
 int sepx_dot_f32(const float *a, const float *b, long long n, double *result);
 
+/* No counterpart in the reference.  The same FP64 dot product with no device
+ * allocation by the library, for callers that cannot let a library allocate
+ * device memory (services that reserve their whole device-memory budget at
+ * start-up, hosts whose own pool owns every allocation).  a, b (b == NULL: the
+ * sum of a) and d_result are device pointers owned by the caller; the work is
+ * enqueued on `stream` (a cudaStream_t; NULL = the default stream) and
+ * d_result is valid once the stream reaches it.  Scratch is a fixed 256 KB
+ * file-scope device array held by every GPU that loads the library: n may be
+ * at most sepx_dot_f32_noalloc_max_elems() (268,435,456) elements, larger
+ * calls are rejected.  All calls share that array; calls that overlap on the
+ * GPU race on it.  The first call on a device looks up the array's address
+ * with that device current and should come before any stream capture. */
+int sepx_dot_f32_noalloc(const float *a, const float *b, long long n, double *d_result,
+                         void *stream);
+long long sepx_dot_f32_noalloc_max_elems(void);
+
 /* Diagnostics and tuning. */
 const char *sepx_last_error(void);
 int sepx_device_error(void);          /* device error word (bounded waits), then cleared */
