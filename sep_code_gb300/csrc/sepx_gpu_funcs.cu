@@ -65,7 +65,7 @@ struct Ctx {
   float *d_damp = nullptr;
   int ntab = 0;
   PropGeom geom;
-  Volume vel, img, F[4], SL[2];
+  Volume vel, img, F[4], SL[2], X;   // X: increment of the linearised pair
   bool vel_set = false;
   int sl_p0 = 0, sl_p1 = 1;   // which SL volume holds the older / newest field
   bool sl_valid = false;
@@ -158,6 +158,7 @@ void free_grid() {
   free_volume(G.vel); free_volume(G.img);
   for (auto &v : G.F) free_volume(v);
   for (auto &v : G.SL) free_volume(v);
+  free_volume(G.X);
   cudaFree(G.d_damp); G.d_damp = nullptr;
   free_pointmap(G.srcmap); free_pointmap(G.recmap);
   G.have_grid = G.vel_set = G.sl_valid = false;
@@ -496,7 +497,8 @@ int loop_lin_source(int jt, int npts, int nt, int js, int prec) {
   return 0;
 }
 
-// traces += R v_t with v from the model in the image buffer
+// traces += R v_t with v from the model in the image buffer (increment form:
+// positions ping-pong between F[0] / F[1], the increment X is updated in place)
 int loop_lin_forward(int jt, int npts, int nt, int js, int prec) {
   RET(need_grid());
   if (!G.vel_set) return fail("transfer_vel_func1 must be called first");
@@ -504,8 +506,8 @@ int loop_lin_forward(int jt, int npts, int nt, int js, int prec) {
   RET(prep_receivers(jt, nt));
   RET(prep_inj(npts, jt, nt, 0, 1.0f));
   if (prec < kSnapF32 || prec > kSnapF16 || js < 1) return fail("invalid snapshot settings");
-  Volume *D0 = &G.F[0], *D1 = &G.F[1], *S0 = &G.F[2], *S1 = &G.F[3];
-  for (auto *v : {D0, D1, S0, S1}) RET(zero_volume(*v));
+  Volume *V0 = &G.F[0], *V1 = &G.F[1], *S0 = &G.F[2], *S1 = &G.F[3], *X = &G.X;
+  for (auto *v : {V0, V1, S0, S1, X}) RET(zero_volume(*v));
   PropParams P = lin_params(js, prec);
   P.src.plane_slot = npts > 0 ? G.srcmap.plane_slot : nullptr;
   P.src.map = G.srcmap.map;
@@ -517,7 +519,9 @@ int loop_lin_forward(int jt, int npts, int nt, int js, int prec) {
   P.nrec = G.rec_nx * G.rec_ny;
   for (int it = 0; it < nt; it++) {
     const int id = it / jt, ii = it - id * jt;
-    set_field(P, 0, *D1, *D0);
+    set_field(P, 0, *V1, *X);   // current position, increment
+    P.out[0] = V0->origin;      // new position
+    P.out2 = X->origin;         // new increment (in place)
     set_field(P, 1, *S1, *S0);
     P.inj_s = G.d_inj + (size_t)it * std::max(npts, 0);
     P.do_snap = P.do_scatter = (it % js == 0);
@@ -525,13 +529,14 @@ int loop_lin_forward(int jt, int npts, int nt, int js, int prec) {
     P.trc_id = id;
     P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
     CKL(launch_prop_step(kLinFwd, P, G.stream));
-    std::swap(D0, D1);
+    std::swap(V0, V1);
     std::swap(S0, S1);
   }
   return 0;
 }
 
-// image := sum_t c u^_t w_t with w from the traces (the exact transpose)
+// image := sum_t c u^_t b_t from the traces: the exact transpose of
+// loop_lin_forward (B ping-pongs between F[0] / F[1], a is updated in F[2])
 int loop_lin_adjoint(int jt, int nt, int js, int prec) {
   RET(need_grid());
   if (!G.vel_set) return fail("transfer_vel_func1 must be called first");
@@ -539,9 +544,10 @@ int loop_lin_adjoint(int jt, int nt, int js, int prec) {
   if (G.snap_nt != nt || G.snap_js != js || G.snap_prec != prec)
     return fail("no source snapshots for nt=%d js=%d prec=%d: run the source pass first", nt, js, prec);
   RET(prep_receivers(jt, nt));
-  Volume *D0 = &G.F[0], *D1 = &G.F[1];
-  RET(zero_volume(*D0));
-  RET(zero_volume(*D1));
+  Volume *B0 = &G.F[0], *B1 = &G.F[1], *A = &G.F[2];
+  RET(zero_volume(*B0));
+  RET(zero_volume(*B1));
+  RET(zero_volume(*A));
   RET(zero_volume(G.img));
   PropParams P = lin_params(js, prec);
   P.rec.plane_slot = G.recmap.plane_slot;
@@ -551,13 +557,15 @@ int loop_lin_adjoint(int jt, int nt, int js, int prec) {
   P.nrec = G.rec_nx * G.rec_ny;
   for (int it = nt - 1; it >= 0; it--) {
     const int id = it / jt, ii = it - id * jt;
-    set_field(P, 0, *D1, *D0);
+    set_field(P, 0, *B1, *A);   // B_{t+1}, a_{t+1}
+    P.out[0] = B0->origin;      // B_t
+    P.out2 = A->origin;         // a_t (in place)
     P.do_snap = P.do_image = (it % js == 0);
     P.snap_index = it / js;
     P.trc_id = id;
     P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
     CKL(launch_prop_step(kLinAdj, P, G.stream));
-    std::swap(D0, D1);
+    std::swap(B0, B1);
   }
   return 0;
 }
@@ -668,6 +676,7 @@ int sepx_create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b, 
     RET(alloc_volume(G.img));
     for (auto &v : G.F) RET(alloc_volume(v));
     for (auto &v : G.SL) RET(alloc_volume(v));
+    RET(alloc_volume(G.X));
   }
   cudaFree(G.d_damp);
   G.d_damp = nullptr;

@@ -47,12 +47,15 @@ struct Mode {
   // sponge passes per step: KW* multiplies at write time, KP* extra multiplies
   // of the previous field; PRE0: field 0 is damped once before the epilogue
   // (kLinFwd: v = T (L(Vv) + 2v - T v_prev) + scattering)
+  // INC0: field 0 is in increment form (kLinFwd, kLinAdj): the previous-field
+  // slot carries the increment and the sponge is applied by the epilogue
+  static constexpr bool INC0 = (MODE == kLinFwd || MODE == kLinAdj);
   static constexpr int KW0 = (MODE == kBornFwd) ? 2
-                             : ((MODE == kSrcProp || MODE == kLinSrc || MODE == kLinFwd) ? 0 : 1);
-  static constexpr int KP0 = (MODE == kLinFwd) ? 1 : KW0;
-  static constexpr bool PRE0 = (MODE == kLinFwd);
+                             : ((MODE == kSrcProp || MODE == kLinSrc || INC0) ? 0 : 1);
+  static constexpr int KP0 = KW0;
+  static constexpr bool PRE0 = false;
   static constexpr int KW1 = (MODE == kBornFwd) ? 1 : 0;
-  static constexpr bool NEED_T = (KW0 > 0 || KP0 > 0 || KW1 > 0 || PRE0);
+  static constexpr bool NEED_T = (KW0 > 0 || KP0 > 0 || KW1 > 0 || PRE0 || INC0);
   static constexpr bool SRC_INJ = (MODE == kSrcProp || MODE == kBornFwd || MODE == kLinSrc ||
                                    MODE == kLinFwd);
   static constexpr int SRC_FIELD = (MODE == kSrcProp || MODE == kLinSrc) ? 0 : 1;
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
       const float *st = smem + s * M::STAGE;
       const int z = za + i;
       float res[NF][4];
-      float4 prevv[NF], velc, imgv = make_float4(0.f, 0.f, 0.f, 0.f), auxv;
+      float4 prevv[NF], velc, imgv = make_float4(0.f, 0.f, 0.f, 0.f), auxv, cur0;
       float vwc[4];
       if (active) {
         // z-queue feed: plane z+4
@@ -320,13 +323,17 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
           if (f == 0 && M::F0_VEL_INSIDE) {
             lap_velin(P.coef, xw, vw, ym, yp, vym, vyp, q[f], sl);
 #pragma unroll
-            for (int c = 0; c < 4; c++) res[f][c] = __fadd_rn(__fadd_rn(sl[c], xw[4 + c]), xw[4 + c]);
+            for (int c = 0; c < 4; c++)
+              res[f][c] = M::INC0 ? sl[c] : __fadd_rn(__fadd_rn(sl[c], xw[4 + c]), xw[4 + c]);
           } else {
             lap_plain(P.coef, xw, ym, yp, q[f], sl);
 #pragma unroll
             for (int c = 0; c < 4; c++)
-              res[f][c] = __fadd_rn(__fmaf_rn(vwc[c], sl[c], xw[4 + c]), xw[4 + c]);
+              res[f][c] = (f == 0 && M::INC0)
+                              ? sl[c]
+                              : __fadd_rn(__fmaf_rn(vwc[c], sl[c], xw[4 + c]), xw[4 + c]);
           }
+          if (f == 0 && M::INC0) cur0 = make_float4(xw[4], xw[5], xw[6], xw[7]);
           prevv[f] = lds4(st + M::PREV + f * kCenterFloats + coff);
         }
         if (load_img) imgv = lds4(st + M::IMG + coff);
@@ -349,11 +356,17 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
           const int kp = (f == 0) ? M::KP0 : M::KW1;
 #pragma unroll
           for (int c = 0; c < 4; c++) {
-            float pv = comp(prevv[f], c);
-            if (kp == 1) pv = damp_k<1>(pv, t[c]);
-            if (kp == 2) pv = damp_k<2>(pv, t[c]);
-            val[f][c] = __fsub_rn(res[f][c], pv);
-            if (f == 0 && M::PRE0) val[f][c] = __fmul_rn(val[f][c], t[c]);
+            if (f == 0 && MODE == kLinFwd) {          // dv_t = T (L(V v) + dv_{t-1})
+              val[f][c] = __fmul_rn(__fadd_rn(res[f][c], comp(prevv[f], c)), t[c]);
+            } else if (f == 0 && MODE == kLinAdj) {   // a_t = T a_{t+1} + V L(B)
+              val[f][c] = __fmaf_rn(vwc[c], res[f][c], __fmul_rn(comp(prevv[f], c), t[c]));
+            } else {
+              float pv = comp(prevv[f], c);
+              if (kp == 1) pv = damp_k<1>(pv, t[c]);
+              if (kp == 2) pv = damp_k<2>(pv, t[c]);
+              val[f][c] = __fsub_rn(res[f][c], pv);
+              if (f == 0 && M::PRE0) val[f][c] = __fmul_rn(val[f][c], t[c]);
+            }
           }
         }
         // source injection into the new field (ids in ascending order)
@@ -409,6 +422,11 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
 
       if (active) {
         const float s6 = (float)0.000001;
+        float vpos[4];
+        if (MODE == kLinAdj) {   // b_t = B_{t+1} + a_t
+#pragma unroll
+          for (int c = 0; c < 4; c++) vpos[c] = __fadd_rn(comp(cur0, c), val[0][c]);
+        }
         if (MODE == kLinSrc && P.do_snap) {
           if (tid == 0) P.snap_scale[blk] = sc;
           if (P.snap_prec == kSnapF32) {
@@ -442,6 +460,12 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
               if (x + c < g.xg)
                 val[0][c] = __fmaf_rn(__fmul_rn(s6, u[c]), comp(imgv, c), val[0][c]);
           }
+          if (MODE == kLinFwd) {   // position v_t = T v_{t-1} + dv_t (val[0] keeps dv_t)
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+              vpos[c] = __fadd_rn(__fmul_rn(comp(cur0, c), t[c]), val[0][c]);
+          }
+          const float *xv = (MODE == kLinFwd) ? vpos : val[0];
           // receiver extraction from the new scattered field
           const int slot = P.rec.plane_slot ? __ldg(P.rec.plane_slot + z) : -1;
           if (slot >= 0) {
@@ -453,7 +477,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
 #pragma unroll
                 for (int k = 0; k < 8; k++) {
                   float *a = tr + (long long)k * P.nrec;
-                  *a = __fmaf_rn(val[0][c], __ldg(P.sinc_row + k), *a);
+                  *a = __fmaf_rn(xv[c], __ldg(P.sinc_row + k), *a);
                 }
               }
             }
@@ -481,14 +505,24 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
 #pragma unroll
             for (int c = 0; c < 4; c++) {
               float iv = comp(imgv, c);
-              o[c] = (x + c < g.xg) ? __fmaf_rn(__fmul_rn(s6, val[0][c]), comp(src, c), iv) : iv;
+              const float w = (MODE == kLinAdj) ? vpos[c] : val[0][c];
+              o[c] = (x + c < g.xg) ? __fmaf_rn(__fmul_rn(s6, w), comp(src, c), iv) : iv;
             }
             *reinterpret_cast<float4 *>(P.img + cell) = make_float4(o[0], o[1], o[2], o[3]);
           }
         }
+        // increment-form field 0: position / increment pair
+        if (M::INC0) {
+          float pos[4];
+#pragma unroll
+          for (int c = 0; c < 4; c++)
+            pos[c] = (MODE == kLinFwd) ? vpos[c] : __fmul_rn(vpos[c], t[c]);   // v_t | B_t = T b_t
+          stcs4(P.out[0] + cell, make_float4(pos[0], pos[1], pos[2], pos[3]));
+          stcs4(P.out2 + cell, make_float4(val[0][0], val[0][1], val[0][2], val[0][3]));
+        }
         // write the new fields with the sponge applied
 #pragma unroll
-        for (int f = 0; f < NF; f++) {
+        for (int f = (M::INC0 ? 1 : 0); f < NF; f++) {
           const int kw = (f == 0) ? M::KW0 : M::KW1;
           float o[4];
 #pragma unroll

@@ -29,12 +29,12 @@ constexpr int kThreads = kConsumerThreads + 32;            // + one TMA producer
 //            given last source wavefield
 //  kLinSrc   source pass of the linearised Born pair: as kSrcProp, and on
 //            snapshot steps the new field is stored compressed
-//  kLinFwd   linearised Born forward: scattered field v_t = T (L(V v) + 2v)
-//            - T^2 v_{t-2} + c u^_t m (u^ = the stored snapshot value,
-//            recomputed bit-identically from the source field carried along),
-//            receiver extraction; the exact transpose of kLinAdj
-//  kLinAdj   linearised adjoint: receiver field as kRtmAdj's, imaging
-//            against the stored snapshots
+//  kLinFwd   linearised Born forward in increment form: dv_t = T (L(V v_{t-1})
+//            + dv_{t-1}) + c u^_t m, v_t = T v_{t-1} + dv_t (u^ = the stored
+//            snapshot value, recomputed bit-identically from the source field
+//            carried along), receiver extraction from v_t
+//  kLinAdj   its exact transpose: a_t = T a_{t+1} + V L(B_{t+1}) + R' d_t,
+//            b_t = B_{t+1} + a_t, image += c u^_t b_t, B_t = T b_t
 enum PropMode : int {
   kSrcProp = 0, kBornFwd = 1, kRtmAdj = 2, kRtmAdj1 = 3, kLinSrc = 4, kLinFwd = 5, kLinAdj = 6
 };
@@ -74,6 +74,7 @@ struct alignas(64) PropParams {
   const float *cur[2];        // logical-origin pointers (z-queue warm-up loads)
   const float *vel;
   float *out[2];              // new fields (the previous-field buffers)
+  float *out2;                // kLinFwd / kLinAdj: the increment (dv / a), updated in place
   float *img;                 // image written back (kRtmAdj, kRtmAdj1)
   PointMap src;               // source points
   const float *inj_s;         // per-step injection values, row of this step
