@@ -73,6 +73,8 @@ int sepx_transfer_sinc_table_d(int nsinc, int ns, float **tables);
 int sepx_transfer_source_func(int npts, int nt, const int *locs, const float *vals);
 int sepx_transfer_receiver_func(int nx, int ny, int nt, const int *locs, const float *vals);
 int sepx_transfer_vel_func1(int nx, int ny, int nz, const float *vel);
+/* receiver geometry with a zeroed device receiver buffer of nt samples */
+int sepx_set_receivers(int nx, int ny, int nt, const int *locs);
 int sepx_transfer_vel_func2(int nx, int ny, int nz, const float *vel);
 int sepx_source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0, float *p1,
                      int jt, int npts, int nt);
@@ -85,8 +87,8 @@ int sepx_rtm_adjoint(int n1, int n2, int n3, int jt, const float *p0_s, const fl
  * return without synchronising.  source_prop keeps its last two wavefields in
  * HBM; rtm_forward reads the image set by sepx_set_image and accumulates into
  * the receiver buffer; rtm_adjoint images into the image buffer, starting
- * from the last source_prop wavefields (use_source_last != 0) or from the ones
- * set with sepx_set_source_fields. */
+ * from the last source_prop wavefields read back swapped as rtm_zero_op does
+ * (use_source_last != 0) or from the ones set with sepx_set_source_fields. */
 int sepx_source_prop_resident(int jt, int npts, int nt);
 int sepx_rtm_forward_resident(int jt, int npts_src, int nt);
 int sepx_rtm_adjoint_resident(int jt, int npts, int nt, int use_source_last);
@@ -132,6 +134,35 @@ int sepx_dot_f32(const float *a, const float *b, long long n, double *result);
 int sepx_dot_f32_noalloc(const float *a, const float *b, long long n, double *d_result,
                          void *stream);
 long long sepx_dot_f32_noalloc_max_elems(void);
+
+/* Per-shot glue of the operator layer, on the context's buffers:
+ * image_to_padded: image buffer := laplac(extract_sub(model)) (model is a
+ *   device float[m3][m2][m1]; model cell = padded cell + (f1,f2,f3));
+ * padded_to_image: model += add_image(laplac'(image buffer));
+ * traces_to_data:  data += deriv(map_data(receiver buffer)) (device
+ *   float[nrec][nt], nt data samples of spacing dt);
+ * data_to_traces:  receiver buffer := map_data'(deriv'(data)).
+ * (Born/rtm_zero_op_3d.cpp:139-166, :248-274 and the helpers they call.) */
+int sepx_op_image_to_padded(const float *model, int m1, int m2, int m3, int f1, int f2, int f3);
+int sepx_op_padded_to_image(float *model, int m1, int m2, int m3, int f1, int f2, int f3);
+int sepx_op_traces_to_data(float *data, int nt, float dt);
+int sepx_op_data_to_traces(const float *data, int nt, float dt);
+
+/* Device float vectors and BLAS-1 on the context stream (hypercube_float,
+ * Born/hypercube_float.cpp:123-223; scale factors applied in double). */
+int sepx_vec_alloc(float **p, long long n);
+int sepx_vec_free(float *p);
+int sepx_vec_upload(float *d, const float *h, long long n);
+int sepx_vec_download(float *h, const float *d, long long n);
+int sepx_vec_copy(float *dst, const float *src, long long n);
+int sepx_vec_fill(float *x, long long n, float v);
+int sepx_vec_scale(float *y, long long n, double a);
+int sepx_vec_scale_add(float *y, const float *x, long long n, double a, double b); /* y = a y + b x */
+int sepx_vec_scale_add2(float *y, const float *x1, const float *x2, long long n, double a,
+                        double b);                                                /* y = a x1 + b x2 */
+int sepx_vec_add(float *y, const float *x, long long n);
+int sepx_vec_mult(float *y, const float *x, long long n);
+int sepx_vec_random(float *y, long long n, unsigned long long seed);   /* uniform(-0.5, 0.5) */
 
 /* Diagnostics and tuning. */
 const char *sepx_last_error(void);

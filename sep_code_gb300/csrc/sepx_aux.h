@@ -16,4 +16,14 @@ cudaError_t launch_point_add(float *p, const long long *off, const float *inj, i
 cudaError_t launch_transpose(const float *in, long long lda, float *out, long long ldb, int rows,
                              int cols, cudaStream_t st);
 
+cudaError_t launch_img_from_model(const float *model, int m1, int m2, int m3, int f1, int f2, int f3,
+                                  float *img, int n1, int n2, int n3, int pitch, cudaStream_t st);
+cudaError_t launch_model_from_img(float *model, int m1, int m2, int m3, int f1, int f2, int f3,
+                                  const float *img, int n1, int n2, int n3, int pitch,
+                                  cudaStream_t st);
+cudaError_t launch_data_from_traces(const float *trc, int nrec, int rnx, int nt, float dt,
+                                    float *data, cudaStream_t st);
+cudaError_t launch_traces_from_data(const float *data, int nrec, int rnx, int nt, int ntrace,
+                                    float dt, float *trc, cudaStream_t st);
+
 }  // namespace sepx

@@ -744,6 +744,22 @@ int sepx_transfer_receiver_func(int nx, int ny, int nt, const int *locs, const f
   return 0;
 }
 
+int sepx_set_receivers(int nx, int ny, int nt, const int *locs) {
+  RET(need_grid());
+  if (nx < 0 || ny < 0 || nt < 1) return fail("invalid receiver shape %d x %d x %d", nx, ny, nt);
+  const int nrec = nx * ny;
+  G.rec_nx = nx;
+  G.rec_ny = ny;
+  G.rec_ntrace = nt;
+  G.ntrace = nt;
+  G.rec_loc.assign(locs, locs + nrec);
+  RET(ensure(&G.d_trc, &G.trc_cap, (size_t)std::max(nrec, 1) * nt));
+  CK(cudaMemsetAsync(G.d_trc, 0, sizeof(float) * (size_t)std::max(nrec, 1) * nt, G.stream));
+  const int nact = (int)std::min<long long>(nrec, (long long)G.n1 * G.n2);
+  RET(build_pointmap(G.recmap, G.rec_loc, nact, "receiver"));
+  return 0;
+}
+
 int sepx_transfer_vel_func1(int nx, int ny, int nz, const float *vel) {
   RET(need_grid());
   RET(check_dims(nx, ny, nz));
@@ -812,9 +828,11 @@ int sepx_rtm_forward_resident(int jt, int npts_src, int nt) {
 int sepx_rtm_adjoint_resident(int jt, int npts, int nt, int use_source_last) {
   RET(need_grid());
   if (use_source_last) {
+    // rtm_zero_op::adjoint reads the two stored fields back swapped: the
+    // newest becomes p0_s (Born/rtm_zero_op_3d.cpp:254-262)
     if (!G.sl_valid) return fail("no source wavefields: run sepx_source_prop_resident first");
-    RET(d2d_volume(G.F[2], G.SL[G.sl_p0]));
-    RET(d2d_volume(G.F[3], G.SL[G.sl_p1]));
+    RET(d2d_volume(G.F[2], G.SL[G.sl_p1]));
+    RET(d2d_volume(G.F[3], G.SL[G.sl_p0]));
   }
   return loop_rtm_adjoint(jt, npts, nt);
 }
@@ -896,6 +914,100 @@ int sepx_dot_f32(const float *a, const float *b, long long n, double *result) {
   CKL(vec_dot(a, b, n, G.d_dot, G.d_dot + np, G.stream));
   CK(cudaMemcpyAsync(result, G.d_dot + np, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
   CK(cudaStreamSynchronize(G.stream));
+  return 0;
+}
+
+// ------------------------------------------------------------ operator glue
+int sepx_op_image_to_padded(const float *model, int m1, int m2, int m3, int f1, int f2, int f3) {
+  RET(need_grid());
+  CKL(launch_img_from_model(model, m1, m2, m3, f1, f2, f3, G.img.origin, G.n1, G.n2, G.n3, G.pitch,
+                            G.stream));
+  return 0;
+}
+
+int sepx_op_padded_to_image(float *model, int m1, int m2, int m3, int f1, int f2, int f3) {
+  RET(need_grid());
+  CKL(launch_model_from_img(model, m1, m2, m3, f1, f2, f3, G.img.origin, G.n1, G.n2, G.n3, G.pitch,
+                            G.stream));
+  return 0;
+}
+
+int sepx_op_traces_to_data(float *data, int nt, float dt) {
+  RET(need_grid());
+  const int nrec = G.rec_nx * G.rec_ny;
+  if (nt < 2 || nt + 4 > G.rec_ntrace) return fail("data length %d does not fit traces of %d", nt, G.rec_ntrace);
+  CKL(launch_data_from_traces(G.d_trc, nrec, G.rec_nx, nt, dt, data, G.stream));
+  return 0;
+}
+
+int sepx_op_data_to_traces(const float *data, int nt, float dt) {
+  RET(need_grid());
+  const int nrec = G.rec_nx * G.rec_ny;
+  if (nt < 2 || nt + 4 > G.rec_ntrace) return fail("data length %d does not fit traces of %d", nt, G.rec_ntrace);
+  CKL(launch_traces_from_data(data, nrec, G.rec_nx, nt, G.rec_ntrace, dt, G.d_trc, G.stream));
+  return 0;
+}
+
+// ------------------------------------------------------------ device vectors (BLAS-1)
+int sepx_vec_alloc(float **p, long long n) {
+  RET(need_device());
+  CK(cudaMalloc((void **)p, sizeof(float) * (size_t)std::max(n, 1LL)));
+  return 0;
+}
+int sepx_vec_free(float *p) {
+  if (p) cudaFree(p);
+  return 0;
+}
+int sepx_vec_upload(float *d, const float *h, long long n) {
+  RET(need_device());
+  CK(cudaMemcpyAsync(d, h, sizeof(float) * n, cudaMemcpyHostToDevice, G.stream));
+  CK(cudaStreamSynchronize(G.stream));
+  return 0;
+}
+int sepx_vec_download(float *h, const float *d, long long n) {
+  RET(need_device());
+  CK(cudaMemcpyAsync(h, d, sizeof(float) * n, cudaMemcpyDeviceToHost, G.stream));
+  CK(cudaStreamSynchronize(G.stream));
+  return 0;
+}
+int sepx_vec_copy(float *dst, const float *src, long long n) {
+  RET(need_device());
+  CK(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, G.stream));
+  return 0;
+}
+int sepx_vec_fill(float *x, long long n, float v) {
+  RET(need_device());
+  CKL(vec_fill(x, n, v, G.stream));
+  return 0;
+}
+int sepx_vec_scale(float *y, long long n, double a) {
+  RET(need_device());
+  CKL(vec_scale(y, n, a, G.stream));
+  return 0;
+}
+int sepx_vec_scale_add(float *y, const float *x, long long n, double a, double b) {
+  RET(need_device());
+  CKL(vec_scale_add(y, x, n, a, b, G.stream));
+  return 0;
+}
+int sepx_vec_scale_add2(float *y, const float *x1, const float *x2, long long n, double a, double b) {
+  RET(need_device());
+  CKL(vec_scale_add2(y, x1, x2, n, a, b, G.stream));
+  return 0;
+}
+int sepx_vec_add(float *y, const float *x, long long n) {
+  RET(need_device());
+  CKL(vec_add(y, x, n, G.stream));
+  return 0;
+}
+int sepx_vec_mult(float *y, const float *x, long long n) {
+  RET(need_device());
+  CKL(vec_mult(y, x, n, G.stream));
+  return 0;
+}
+int sepx_vec_random(float *y, long long n, unsigned long long seed) {
+  RET(need_device());
+  CKL(vec_random(y, n, seed, G.stream));
   return 0;
 }
 
