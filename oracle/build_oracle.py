@@ -94,6 +94,7 @@ def build_ref(force: bool = False) -> Path | None:
     stubs = HERE / "ref_stubs"
     srcs = [born / s for s in REF_SOURCES]
     mine = [stubs / "ref_shim.cpp", stubs / "sep_stubs.cpp", stubs / "ref_gpu_stubs.cpp",
+            stubs / "ref_alloc.cpp",
             stubs / "seplib.h", stubs / "sep3d.h", HERE / "sepx_oracle.c", HERE / "sepx_oracle.h",
             HERE / "sepx_oracle_loops.inc"]
     if not force and _newer(REF_SO, srcs + mine + [Path(__file__)]):
@@ -103,7 +104,8 @@ def build_ref(force: bool = False) -> Path | None:
               "-include", "ctime", "-include", "cmath", "-include", "cstring",
               f"-I{stubs}", f"-I{born}"]
     jobs = []
-    for src in srcs + [stubs / "ref_shim.cpp", stubs / "sep_stubs.cpp", stubs / "ref_gpu_stubs.cpp"]:
+    for src in srcs + [stubs / "ref_shim.cpp", stubs / "sep_stubs.cpp", stubs / "ref_gpu_stubs.cpp",
+                       stubs / "ref_alloc.cpp"]:
         obj = REF_OUT / (src.stem + ".o")
         objs.append(obj)
         if src.name in PATCH_RETURNS:
@@ -124,8 +126,10 @@ def build_ref(force: bool = False) -> Path | None:
     bad = [j for j in jobs if j.wait() != 0]
     if bad:
         raise RuntimeError("reference host build failed")
-    subprocess.run(["g++", "-shared", "-fopenmp", "-o", str(REF_SO), *map(str, objs), "-lm"],
-                   check=True)
+    # -Bsymbolic-functions: the zero-tailed new[] of ref_alloc.cpp serves this
+    # library's own allocations only
+    subprocess.run(["g++", "-shared", "-fopenmp", "-Wl,-Bsymbolic-functions", "-o", str(REF_SO),
+                    *map(str, objs), "-lm"], check=True)
     for o in objs:
         o.unlink()
     return REF_SO
