@@ -54,6 +54,7 @@ struct Ctx {
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   long long launches = 0;
   int zchunk_override = 0;
+  int num_sms = 152;
   std::string err;
   // grid
   bool have_grid = false;
@@ -273,22 +274,32 @@ int build_pointmap(PointMapDev &m, const std::vector<int> &loc, int npts, const 
   return 0;
 }
 
-int auto_zchunk() {
+// Planes per CTA along z.  Longer chunks amortise the 8-plane warm-up of the
+// z-queues; shorter ones balance the waves.  Measured on GB300 at 560x560x496:
+// source_prop and the Born forward are best near 80 planes, the RTM adjoint
+// near 32.  Small grids shorten the chunk until there are two waves of
+// 3 CTAs per SM.
+int auto_zchunk(int mode) {
   if (G.zchunk_override > 0) return G.zchunk_override;
   const PropGeom &g = G.geom;
-  const int tiles = ((g.xe - g.xb + kTX - 1) / kTX) * ((g.ye - g.yb + kTY - 1) / kTY);
+  const long long tiles = (long long)((g.xe - g.xb + kTX - 1) / kTX) * ((g.ye - g.yb + kTY - 1) / kTY);
   const int depth = std::max(1, g.ze - g.zb);
-  int nch = std::max(1, (8 * 152 + tiles - 1) / std::max(tiles, 1));
-  int zc = (depth + nch - 1) / nch;
-  zc = std::max(zc, 32);
-  return std::min(zc, depth);
+  int zc = (mode == kRtmAdj || mode == kRtmAdj1 || mode == kLinAdj) ? 32 : 80;
+  while (zc > 16 && tiles * ((depth + zc - 1) / zc) < 2LL * 3 * G.num_sms) zc /= 2;
+  return std::max(1, std::min(zc, depth));
+}
+
+// One fused step with the mode's z-chunk.
+cudaError_t launch_step(int mode, const PropParams &P0) {
+  PropParams P = P0;
+  P.g.zchunk = auto_zchunk(mode);
+  return launch_prop_step(mode, P, G.stream);
 }
 
 PropParams base_params() {
   PropParams P;
   memset(&P, 0, sizeof(P));
   P.g = G.geom;
-  P.g.zchunk = auto_zchunk();
   memcpy(P.coef, G.coef, sizeof(G.coef));
   P.damp_tab = G.d_damp;
   P.ntab = G.ntab;
@@ -363,7 +374,7 @@ int loop_source_prop(int jt, int npts, int nt) {
     set_field(P, 0, *B, *A);
     P.inj_s = G.d_inj + (size_t)it * std::max(npts, 0);
     if (npts <= 0) P.src.plane_slot = nullptr;
-    CKL(launch_prop_step(kSrcProp, P, G.stream));
+    CKL(launch_step(kSrcProp, P));
     std::swap(A, B);
   }
   G.sl_p0 = (A == &G.SL[0]) ? 0 : 1;
@@ -397,7 +408,7 @@ int loop_rtm_forward(int jt, int npts_src, int nt) {
     P.do_scatter = (it % jt == 0);
     P.trc_id = id;
     P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
-    CKL(launch_prop_step(kBornFwd, P, G.stream));
+    CKL(launch_step(kBornFwd, P));
     std::swap(D0, D1);
     std::swap(S0, S1);
   }
@@ -429,10 +440,10 @@ int loop_rtm_adjoint(int jt, int npts, int nt) {
     set_field(P, 0, *D1, *D0);
     if (it == nt - 1) {
       P.tm_aux_c = S0->tm_c;
-      CKL(launch_prop_step(kRtmAdj1, P, G.stream));
+      CKL(launch_step(kRtmAdj1, P));
     } else {
       set_field(P, 1, *S1, *S0);
-      CKL(launch_prop_step(kRtmAdj, P, G.stream));
+      CKL(launch_step(kRtmAdj, P));
       if (npts > 0)
         CKL(launch_point_add(S1->origin, G.srcmap.off, G.d_inj + (size_t)it * npts, npts, G.stream));
       std::swap(S0, S1);
@@ -488,7 +499,7 @@ int loop_lin_source(int jt, int npts, int nt, int js, int prec) {
     P.inj_s = G.d_inj + (size_t)it * std::max(npts, 0);
     P.do_snap = (it % js == 0);
     P.snap_index = it / js;
-    CKL(launch_prop_step(kLinSrc, P, G.stream));
+    CKL(launch_step(kLinSrc, P));
     std::swap(A, B);
   }
   G.snap_js = js;
@@ -528,7 +539,7 @@ int loop_lin_forward(int jt, int npts, int nt, int js, int prec) {
     P.snap_index = it / js;
     P.trc_id = id;
     P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
-    CKL(launch_prop_step(kLinFwd, P, G.stream));
+    CKL(launch_step(kLinFwd, P));
     std::swap(V0, V1);
     std::swap(S0, S1);
   }
@@ -564,7 +575,7 @@ int loop_lin_adjoint(int jt, int nt, int js, int prec) {
     P.snap_index = it / js;
     P.trc_id = id;
     P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
-    CKL(launch_prop_step(kLinAdj, P, G.stream));
+    CKL(launch_step(kLinAdj, P));
     std::swap(B0, B1);
   }
   return 0;
@@ -623,6 +634,7 @@ int sepx_setup_cuda(int ngpus) {
   CK(cudaGetDeviceCount(&ndev));
   if (ndev < 1) return fail("no CUDA device");
   CK(cudaSetDevice(0));
+  CK(cudaDeviceGetAttribute(&G.num_sms, cudaDevAttrMultiProcessorCount, 0));
   CK(cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking));
   CK(cudaMalloc((void **)&G.d_err, sizeof(int)));
   CK(cudaMemsetAsync(G.d_err, 0, sizeof(int), G.stream));
@@ -656,12 +668,14 @@ int sepx_create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b, 
                          c00(c) / 63.0, -c00(a) / 896.0, -c00(b) / 896.0, -c00(c) / 896.0};
   for (int k = 0; k < 13; k++) G.coef[k] = (float)cd[k];
   // sponge factor by edge distance: expf(-bc_b*(bc_a-edge)) when < 1
-  G.ntab = std::max(n1, std::max(n2, n3)) / 2 + 1;
-  std::vector<float> tab(G.ntab);
-  for (int e = 0; e < G.ntab; e++) {
+  int ntab_all = std::max(n1, std::max(n2, n3)) / 2 + 1;
+  std::vector<float> tab(ntab_all);
+  G.ntab = 0;   // entries past the last factor < 1 are 1: the kernels stop there
+  for (int e = 0; e < ntab_all; e++) {
     const float arg = -bc_b * (bc_a - (float)e);
     const float t = (float)std::exp((double)arg);
     tab[e] = (t < 1.0f) ? t : 1.0f;
+    if (tab[e] < 1.0f) G.ntab = e + 1;
   }
   PropGeom &g = G.geom;
   g.n1 = n1; g.n2 = n2; g.n3 = n3; g.pitch = G.pitch; g.plane = G.plane;
@@ -680,8 +694,9 @@ int sepx_create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b, 
   }
   cudaFree(G.d_damp);
   G.d_damp = nullptr;
-  CK(cudaMalloc((void **)&G.d_damp, sizeof(float) * G.ntab));
-  CK(cudaMemcpyAsync(G.d_damp, tab.data(), sizeof(float) * G.ntab, cudaMemcpyHostToDevice, G.stream));
+  CK(cudaMalloc((void **)&G.d_damp, sizeof(float) * std::max(G.ntab, 1)));
+  if (G.ntab > 0)
+    CK(cudaMemcpyAsync(G.d_damp, tab.data(), sizeof(float) * G.ntab, cudaMemcpyHostToDevice, G.stream));
   CK(cudaStreamSynchronize(G.stream));
   G.have_grid = true;
   // geometry changed: point maps are rebuilt on the next transfer

@@ -34,6 +34,22 @@
 #include "sepx_device.cuh"
 #include "sepx_prop.h"
 
+// Resident CTAs per SM the register budget targets, and ring depths, of the
+// two heaviest modes (compile-time tuning knobs; the defaults measured best
+// on GB300 at 560x560x496).
+#ifndef SEPX_FWD_MINB
+#define SEPX_FWD_MINB 3
+#endif
+#ifndef SEPX_ADJ_MINB
+#define SEPX_ADJ_MINB 3
+#endif
+#ifndef SEPX_FWD_STAGES
+#define SEPX_FWD_STAGES 3
+#endif
+#ifndef SEPX_ADJ_STAGES
+#define SEPX_ADJ_STAGES 3
+#endif
+
 namespace sepx {
 
 template <int MODE>
@@ -75,6 +91,12 @@ struct Mode {
             (VEL_HALO ? kHaloFloats : kCenterFloats) + NF * kCenterFloats +
             (HAS_AUX ? kCenterFloats : 0));
   static constexpr uint32_t BYTES_IMG = BYTES_NOIMG + (HAS_IMG ? 4u * kCenterFloats : 0u);
+  // resident blocks per SM the register budget is sized for
+  static constexpr int MINB = (MODE == kSrcProp)  ? 4
+                              : (MODE == kBornFwd) ? SEPX_FWD_MINB
+                              : (MODE == kRtmAdj)  ? SEPX_ADJ_MINB
+                              : (MODE == kLinFwd)  ? 2
+                                                   : 3;
 };
 
 // ---- compressed snapshots: power-of-two max-abs scale per 32x16 block-plane ----
@@ -113,16 +135,26 @@ __device__ __forceinline__ float consumer_max(float m, float *red, int warp, int
 
 // Sponge factor of damp_kernel (Born/wave_fkernel.3d8o.cu:183-210), one GPU:
 // cells with x < xg, y < yg and edge = distance to the nearest face minus 4
-// >= 0; 1 elsewhere.
-__device__ __forceinline__ float sponge(const PropParams &P, int x, int y, int z) {
+// >= 0 take tab[edge]; 1 elsewhere.
+// Sponge from the z-invariant part exy = min over the x/y faces of the
+// distance minus 4, clamped to 254, four columns packed one byte each; 255
+// marks a cell outside the sponge region x < xg, y < yg (factor 1 at every
+// z).  Inside, e = min(exy, z-4, n3-4-z).  The table (entries < 1 only,
+// ntab <= kTabSmem, so a clamped 254 never indexes it) sits in shared memory;
+// a longer table takes the per-cell path from global memory.
+constexpr int kTabSmem = 254;
+
+__device__ __forceinline__ int sponge_exy(const PropGeom &g, int x, int y) {
+  if (x >= g.xg || y >= g.yg) return 255;
+  const int e = min(min(x - 4, g.n1 - 4 - x), min(y - 4, g.n2 - 4 - y));
+  return min(e, 254);   // e >= 0 here: x, y lie in the interior
+}
+
+__device__ __forceinline__ float sponge_full(const PropParams &P, int x, int y, int z) {
   const PropGeom &g = P.g;
   if (x >= g.xg || y >= g.yg) return 1.0f;
-  int e = x - 4;
-  e = min(e, z - 4);
-  e = min(e, g.n2 - 4 - y);
-  e = min(e, g.n1 - 4 - x);
-  e = min(e, g.n3 - 4 - z);
-  e = min(e, y - 4);
+  int e = x - 4; e = min(e, z - 4); e = min(e, g.n2 - 4 - y); e = min(e, g.n1 - 4 - x);
+  e = min(e, g.n3 - 4 - z); e = min(e, y - 4);
   if (e < 0 || e >= P.ntab) return 1.0f;
   return __ldg(P.damp_tab + e);
 }
@@ -196,7 +228,7 @@ __device__ __forceinline__ float4 mul4(float4 a, float4 b) {
 }
 
 template <int MODE, int STAGES>
-__global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_constant__ PropParams P) {
+__global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(const __grid_constant__ PropParams P) {
   using M = Mode<MODE>;
   constexpr int NF = M::NF;
   // dynamic shared memory only: [<=127 B pad][STAGES stages][full bars][empty bars]
@@ -206,6 +238,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
   unsigned long long *bar_full = reinterpret_cast<unsigned long long *>(smem + STAGES * M::STAGE);
   unsigned long long *bar_empty = bar_full + STAGES;
   float *red = reinterpret_cast<float *>(bar_empty + STAGES);   // 4 floats: block max
+  float *tab_s = red + 4;                                       // kTabSmem floats: sponge
 
   const PropGeom &g = P.g;
   const int tid = threadIdx.x;
@@ -272,6 +305,20 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
     const int x = x0 + 4 * xq, y = y0 + row;
     const bool active = (x < g.xe);
     const long long rowoff = (long long)x + (long long)g.pitch * y;
+    uint32_t exy4 = 0;   // packed z-invariant sponge distances of the 4 columns
+    if (M::NEED_T) {
+      if (P.ntab <= kTabSmem)
+        for (int e = tid; e < P.ntab; e += kConsumerThreads) tab_s[e] = __ldg(P.damp_tab + e);
+#pragma unroll
+      for (int c = 0; c < 4; c++) exy4 |= (uint32_t)sponge_exy(g, x + c, y) << (8 * c);
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+    }
+    // per-plane point-map slots, fetched one plane ahead
+    auto src_slot = [&](int zz) { return (M::SRC_INJ && P.src.plane_slot) ? __ldg(P.src.plane_slot + zz) : -1; };
+    auto rec_slot = [&](int zz) {
+      return ((M::REC_INJECT || M::REC_EXTRACT) && P.rec.plane_slot) ? __ldg(P.rec.plane_slot + zz) : -1;
+    };
+    int src_next = src_slot(za), rec_next = rec_slot(za);
     float4 q[NF][9];
     // warm-up: planes za-4 .. za+3 of the current field(s) along z
     if (active) {
@@ -294,6 +341,11 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
         break;
       const float *st = smem + s * M::STAGE;
       const int z = za + i;
+      const int src_sl = src_next, rec_sl = rec_next;
+      if (i + 1 < niter) {
+        src_next = src_slot(z + 1);
+        rec_next = rec_slot(z + 1);
+      }
       float res[NF][4];
       float4 prevv[NF], velc, imgv = make_float4(0.f, 0.f, 0.f, 0.f), auxv, cur0;
       float vwc[4];
@@ -348,8 +400,18 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
       const long long cell = rowoff + g.plane * z;
       if (active) {
         if (M::NEED_T) {
+          if (P.ntab <= kTabSmem) {
+            const int zd = min(z - 4, g.n3 - 4 - z);
 #pragma unroll
-          for (int c = 0; c < 4; c++) t[c] = sponge(P, x + c, y, z);
+            for (int c = 0; c < 4; c++) {
+              const int ex = (int)((exy4 >> (8 * c)) & 255u);
+              const int e = min(ex, zd);
+              t[c] = (ex != 255 && e >= 0 && e < P.ntab) ? tab_s[e] : 1.0f;
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < 4; c++) t[c] = sponge_full(P, x + c, y, z);
+          }
         }
 #pragma unroll
         for (int f = 0; f < NF; f++) {
@@ -370,8 +432,8 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
           }
         }
         // source injection into the new field (ids in ascending order)
-        if (M::SRC_INJ && P.src.plane_slot) {
-          const int slot = __ldg(P.src.plane_slot + z);
+        if (M::SRC_INJ) {
+          const int slot = src_sl;
           if (slot >= 0) {
             const int *mp = P.src.map + (long long)slot * g.n1 * g.n2 + (long long)y * g.n1 + x;
 #pragma unroll
@@ -382,8 +444,8 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
           }
         }
         // receiver injection (adjoint): time-major traces, 8 taps
-        if (M::REC_INJECT && P.rec.plane_slot) {
-          const int slot = __ldg(P.rec.plane_slot + z);
+        if (M::REC_INJECT) {
+          const int slot = rec_sl;
           if (slot >= 0) {
             const int *mp = P.rec.map + (long long)slot * g.n1 * g.n2 + (long long)y * g.n1 + x;
 #pragma unroll
@@ -467,7 +529,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
           }
           const float *xv = (MODE == kLinFwd) ? vpos : val[0];
           // receiver extraction from the new scattered field
-          const int slot = P.rec.plane_slot ? __ldg(P.rec.plane_slot + z) : -1;
+          const int slot = rec_sl;
           if (slot >= 0) {
             const int *mp = P.rec.map + (long long)slot * g.n1 * g.n2 + (long long)y * g.n1 + x;
 #pragma unroll
@@ -556,7 +618,7 @@ __global__ void __launch_bounds__(kThreads) prop_step_kernel(const __grid_consta
 
 template <int MODE, int STAGES>
 constexpr size_t smem_bytes_of() {
-  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 16 + 128;
+  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 16 + 4 * kTabSmem + 128;
 }
 
 template <int MODE, int STAGES>
@@ -581,8 +643,8 @@ cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
   dim3 grid((wx + kTX - 1) / kTX, (wy + kTY - 1) / kTY, (wz + g.zchunk - 1) / g.zchunk);
   switch (mode) {
     case kSrcProp: return launch_mode<kSrcProp, 4>(P, grid, st);
-    case kBornFwd: return launch_mode<kBornFwd, 3>(P, grid, st);
-    case kRtmAdj: return launch_mode<kRtmAdj, 3>(P, grid, st);
+    case kBornFwd: return launch_mode<kBornFwd, SEPX_FWD_STAGES>(P, grid, st);
+    case kRtmAdj: return launch_mode<kRtmAdj, SEPX_ADJ_STAGES>(P, grid, st);
     case kRtmAdj1: return launch_mode<kRtmAdj1, 3>(P, grid, st);
     case kLinSrc: return launch_mode<kLinSrc, 4>(P, grid, st);
     case kLinFwd: return launch_mode<kLinFwd, 3>(P, grid, st);
@@ -594,8 +656,8 @@ cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
 size_t prop_smem_bytes(int mode) {
   switch (mode) {
     case kSrcProp: return smem_bytes_of<kSrcProp, 4>();
-    case kBornFwd: return smem_bytes_of<kBornFwd, 3>();
-    case kRtmAdj: return smem_bytes_of<kRtmAdj, 3>();
+    case kBornFwd: return smem_bytes_of<kBornFwd, SEPX_FWD_STAGES>();
+    case kRtmAdj: return smem_bytes_of<kRtmAdj, SEPX_ADJ_STAGES>();
     case kRtmAdj1: return smem_bytes_of<kRtmAdj1, 3>();
     case kLinSrc: return smem_bytes_of<kLinSrc, 4>();
     case kLinFwd: return smem_bytes_of<kLinFwd, 3>();
