@@ -15,6 +15,7 @@ enum DevErr : int {
   kErrFullWait = 1,    // consumer gave up waiting for a TMA stage
   kErrEmptyWait = 2,   // producer gave up waiting for consumers to free a stage
   kErrDrainWait = 3,   // exit-time wait for in-flight copies gave up
+  kErrMmaWait = 4,     // wait for tensor-core MMAs to finish gave up
 };
 
 constexpr unsigned long long kWaitBudgetNs = 2000000000ull;  // 2 s

@@ -1,0 +1,104 @@
+// sepx_tc.cuh -- fifth-generation tensor-core (tcgen05) building blocks for
+// sm_103a: tensor-memory allocation, shared-memory matrix descriptors, the
+// BF16 MMA with FP32 accumulation in tensor memory, and the loads that bring
+// the accumulator back to registers.  Inline PTX only.
+//
+// Operand layout used throughout ("no swizzle" canonical layout): a core
+// matrix is 8 rows x 16 bytes (8 BF16), stored contiguously (128 B).  For a
+// K-major operand the rows are M (or N) and the 16 bytes run along K; for an
+// MN-major operand the rows are K and the 16 bytes run along M (or N).  Core
+// matrices are placed at  (kgroup * ngroups_mn + group_mn) * 128  bytes, so
+// the stride between neighbouring MN groups is 128 B and the stride between
+// neighbouring K groups is ngroups_mn * 128 B.
+#pragma once
+#include <cstdint>
+
+namespace sepx {
+namespace tc {
+
+// ---- shared-memory matrix descriptor (64 bit) ----
+// bits 0-13 start address >> 4; 16-29 leading-dimension byte offset >> 4;
+// 32-45 stride-dimension byte offset >> 4; 46-47 descriptor version (1);
+// 49-51 base offset (0); 52 LBO mode (0); 61-63 layout (0 = no swizzle).
+// No swizzle, K-major:  LBO = stride between K groups, SBO = between M/N groups.
+// No swizzle, MN-major: LBO = stride between K groups, SBO = between M/N groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// ---- instruction descriptor, kind::f16 with BF16 inputs and FP32 accumulator ----
+// bits 4-5 D format (1 = F32); 7-9 A format (1 = BF16); 10-12 B format
+// (1 = BF16); 15 A major (0 K, 1 MN); 16 B major; 17-22 N >> 3; 24-28 M >> 4.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// ---- tensor memory ----
+// One warp allocates `ncols` (a power of two >= 32) columns; the base address
+// is written to shared memory at `dst`.
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, M x N x 16, issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// the mbarrier completes one phase once every MMA issued so far by this thread is done
+__device__ __forceinline__ void mma_commit(uint32_t mbar_smem) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_smem)
+      : "memory");
+}
+
+// 32 lanes x 16 columns of 32-bit accumulator: thread t of the warp receives
+// lane (32 * (warp % 4) + t), columns col .. col+15.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  // load and wait in one block: the registers are valid only after the wait
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+}  // namespace sepx

@@ -1,0 +1,723 @@
+// sepx_unet.cu -- kernels of the learned preconditioner (a 3-D U-Net applied
+// to the least-squares RTM search direction): 3x3x3 (or 1x1x1) convolutions
+// as implicit GEMMs on the fifth-generation tensor cores -- BF16 operands in
+// shared memory, FP32 accumulators in tensor memory -- for the forward pass,
+// the data gradient (the same kernel with flipped, transposed weights) and the
+// weight gradient; plus the memory-bound pieces around them (2x2x2 average
+// pooling, nearest upsampling, ReLU masks, loss, Adam, weight packing).
+//
+// Activations are channel-last BF16 volumes: element (n, z, y, x, c) of a view
+// lives at base[(((n*D + z)*H + y)*W + x)*cstride + coff + c]; channel counts,
+// strides and offsets are multiples of 8, so 8 channels are one 16-byte load.
+// Concatenation is a wider buffer whose channel slices are separate views.
+//
+// GEMM shapes: forward / data gradient  M = voxels (tiles of 128),
+// N = output channels (16..128), K = taps x input channels (chunks of 64);
+// weight gradient  M = taps x input channels (tiles of 128), N = output
+// channels, K = voxels (chunks of 64, split over CTAs, FP32 atomics).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sepx_common.h"
+#include "sepx_device.cuh"
+#include "sepx_tc.cuh"
+#include "sepx_unet.h"
+
+namespace sepx {
+
+constexpr int kTM = 128;   // GEMM rows per CTA (tensor-memory lanes)
+constexpr int kKC = 64;    // K per pipeline stage (8 K groups of 8)
+constexpr int kUThreads = 128;
+constexpr int kMaxN = 128;
+// spare shared memory after the two stages, so that operand reads through the
+// descriptors stay inside the CTA's allocation whatever the group strides
+constexpr int kSmemSlack = 64 * 1024;
+
+struct View {
+  const __nv_bfloat16 *p;
+  int cstride, coff;
+};
+
+__device__ __forceinline__ void tap_offset(int t, int ntap, int &dz, int &dy, int &dx) {
+  if (ntap == 1) {
+    dz = dy = dx = 0;
+  } else {
+    dz = t / 9 - 1;
+    dy = (t / 3) % 3 - 1;
+    dx = t % 3 - 1;
+  }
+}
+
+// 16 bytes (8 channels) of voxel v shifted by tap t, or zeros outside the volume
+__device__ __forceinline__ uint4 gather8(const View &x, long long v, int D, int H, int W, int t,
+                                         int ntap, int c0) {
+  int dz, dy, dx;
+  tap_offset(t, ntap, dz, dy, dx);
+  const int xx = (int)(v % W);
+  const int yy = (int)((v / W) % H);
+  const int zz = (int)((v / ((long long)W * H)) % D);
+  const int x2 = xx + dx, y2 = yy + dy, z2 = zz + dz;
+  if (x2 < 0 || x2 >= W || y2 < 0 || y2 >= H || z2 < 0 || z2 >= D) return make_uint4(0, 0, 0, 0);
+  const long long v2 = v + (long long)dz * H * W + (long long)dy * W + dx;
+  return *reinterpret_cast<const uint4 *>(x.p + v2 * x.cstride + x.coff + c0);
+}
+
+// ---------------------------------------------------------------------------
+// Forward (and data-gradient) convolution.
+//   Y[v][n] = act( sum_{t, c} X[v + off(t)][c] * Wt[n][t*cin + c] + bias[n] )
+// wp: packed weights [kchunks][8][np/8][8 n][8 k] BF16 (K-major operand B).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
+    View x, int nb, int D, int H, int W, int cin, int ntap, const __nv_bfloat16 *__restrict__ wp,
+    int kchunks, const float *__restrict__ bias, int cout, int np, int relu, __nv_bfloat16 *y,
+    int y_cstride, int y_coff, float *yf, const float *resid, int *err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  const int a_bytes = kTM * kKC * 2;      // 16 KB
+  const int b_bytes = np * kKC * 2;       // <= 16 KB
+  const int stage_bytes = a_bytes + b_bytes;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + 2 * stage_bytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long V = (long long)nb * D * H * W;
+  const long long v0 = (long long)blockIdx.x * kTM;
+  const uint32_t ncols = np <= 32 ? 32 : (np <= 64 ? 64 : 128);
+
+  if (warp == 0) {
+    tc::tmem_alloc(smem_u32(tslot), ncols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(&bar[0]), 1);
+    mbar_init(smem_u32(&bar[1]), 1);
+    mbar_fence_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(kTM, np, false, false);
+  const int ngn = np / 8;
+  bool ok = true;
+  int last = -1;   // last chunk whose MMAs were committed
+
+  for (int j = 0; j < kchunks; j++) {
+    const int s = j & 1;
+    if (j >= 2) {
+      // the MMAs of chunk j-2 have read this stage
+      if (!mbar_wait_bounded(smem_u32(&bar[s]), ((j - 2) >> 1) & 1, err, kErrMmaWait)) ok = false;
+    }
+    if (!__syncthreads_and(ok)) break;
+    unsigned char *A = sm + s * stage_bytes;
+    unsigned char *B = A + a_bytes;
+    // A: row = tid (one output voxel), 8 K groups of 8 channels of one tap
+    {
+      const int r = tid;
+      const long long v = v0 + r;
+#pragma unroll
+      for (int kg = 0; kg < kKC / 8; kg++) {
+        const int k0 = j * kKC + kg * 8;
+        const int t = k0 / cin, c0 = k0 - t * cin;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (v < V && t < ntap) val = gather8(x, v, D, H, W, t, ntap, c0);
+        *reinterpret_cast<uint4 *>(A + (kg * (kTM / 8) + (r >> 3)) * 128 + (r & 7) * 16) = val;
+      }
+    }
+    // B: this chunk's packed weights, copied as they are
+    {
+      const uint4 *src = reinterpret_cast<const uint4 *>(wp + (size_t)j * np * kKC);
+      uint4 *dst = reinterpret_cast<uint4 *>(B);
+      for (int i = tid; i < b_bytes / 16; i += kUThreads) dst[i] = src[i];
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+#pragma unroll
+      for (int k16 = 0; k16 < kKC / 16; k16++) {
+        const uint64_t ad = tc::smem_desc(a0 + k16 * 2 * (kTM / 8) * 128, (kTM / 8) * 128, 128);
+        const uint64_t bd = tc::smem_desc(b0 + k16 * 2 * ngn * 128, ngn * 128, 128);
+        tc::mma_bf16(tmem, ad, bd, idesc, (j > 0 || k16 > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(smem_u32(&bar[s]));
+    }
+    last = j;
+  }
+  // all MMAs done (also on the error path, before the tensor memory is
+  // freed): the last commit covers every earlier one
+  if (last >= 0) {
+    if (!mbar_wait_bounded(smem_u32(&bar[last & 1]), (last >> 1) & 1, err, kErrMmaWait)) ok = false;
+  }
+  if (last != kchunks - 1) ok = false;
+  ok = __syncthreads_and(ok);
+  tc::fence_after_sync();
+  if (ok) {
+    // epilogue: warp w holds voxels 32w..32w+31 of the tile (TMEM lanes)
+    const long long v = v0 + warp * 32 + lane;
+    for (int n0 = 0; n0 < np; n0 += 16) {
+      float acc[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + n0, acc);
+      if (v < V) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const int n = n0 + i;
+          float o = acc[i] + ((n < cout && bias) ? bias[n] : 0.f);
+          if (relu) o = fmaxf(o, 0.f);
+          acc[i] = o;
+        }
+        if (y) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 8) {
+            if (n0 + i + 8 <= cout) {
+              __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+              for (int e = 0; e < 8; e++) h[e] = __float2bfloat16_rn(acc[i + e]);
+              *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff + n0 + i) =
+                  *reinterpret_cast<const uint4 *>(h);
+            }
+          }
+        }
+        if (yf) {
+#pragma unroll
+          for (int i = 0; i < 16; i++)
+            if (n0 + i < cout)
+              yf[v * cout + n0 + i] = acc[i] + (resid ? resid[v * cout + n0 + i] : 0.f);
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient:  dW[m][n] += sum_v X[v + off(t)][c] * dY[v][n],  m = t*cin + c.
+// A (M = taps x channels, K = voxels) and B (N = channels of dY, K = voxels)
+// are MN-major: 8 consecutive channels of one voxel are one 16-byte row.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
+    View x, int nb, int D, int H, int W, int cin, int ntap, View dy, int cout, int np,
+    int vchunks_per_cta, float *dw, int *err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  const int a_bytes = kTM * kKC * 2;
+  const int b_bytes = np * kKC * 2;
+  const int stage_bytes = a_bytes + b_bytes;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + 2 * stage_bytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long V = (long long)nb * D * H * W;
+  const int mtot = ntap * cin;
+  const int m0 = blockIdx.x * kTM;
+  const long long vchunks = (V + kKC - 1) / kKC;
+  const long long jb = (long long)blockIdx.y * vchunks_per_cta;
+  const int nch = (int)min((long long)vchunks_per_cta, vchunks - jb);
+  const uint32_t ncols = np <= 32 ? 32 : (np <= 64 ? 64 : 128);
+  if (nch <= 0) return;   // uniform for the CTA, before any allocation
+
+  if (warp == 0) {
+    tc::tmem_alloc(smem_u32(tslot), ncols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(&bar[0]), 1);
+    mbar_init(smem_u32(&bar[1]), 1);
+    mbar_fence_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(kTM, np, true, true);
+  const int ngn = np / 8;
+  bool ok = true;
+  int last = -1;
+
+  for (int jj = 0; jj < nch; jj++) {
+    const int s = jj & 1;
+    if (jj >= 2) {
+      if (!mbar_wait_bounded(smem_u32(&bar[s]), ((jj - 2) >> 1) & 1, err, kErrMmaWait)) ok = false;
+    }
+    if (!__syncthreads_and(ok)) break;
+    unsigned char *A = sm + s * stage_bytes;
+    unsigned char *B = A + a_bytes;
+    const long long vb = (jb + jj) * kKC;
+    // A: 16 M groups x 64 voxels of 16 bytes
+    for (int p = tid; p < (kTM / 8) * kKC; p += kUThreads) {
+      const int mg = p % (kTM / 8), kv = p / (kTM / 8);
+      const int m = m0 + mg * 8;
+      const long long v = vb + kv;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (m < mtot && v < V) {
+        const int t = m / cin, c0 = m - t * cin;
+        val = gather8(x, v, D, H, W, t, ntap, c0);
+      }
+      *reinterpret_cast<uint4 *>(A + ((kv >> 3) * (kTM / 8) + mg) * 128 + (kv & 7) * 16) = val;
+    }
+    // B: np/8 N groups x 64 voxels of dY
+    for (int p = tid; p < ngn * kKC; p += kUThreads) {
+      const int ng = p % ngn, kv = p / ngn;
+      const long long v = vb + kv;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (v < V && ng * 8 < cout)
+        val = *reinterpret_cast<const uint4 *>(dy.p + v * dy.cstride + dy.coff + ng * 8);
+      *reinterpret_cast<uint4 *>(B + ((kv >> 3) * ngn + ng) * 128 + (kv & 7) * 16) = val;
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+#pragma unroll
+      for (int k16 = 0; k16 < kKC / 16; k16++) {
+        const uint64_t ad = tc::smem_desc(a0 + k16 * 2 * (kTM / 8) * 128, (kTM / 8) * 128, 128);
+        const uint64_t bd = tc::smem_desc(b0 + k16 * 2 * ngn * 128, ngn * 128, 128);
+        tc::mma_bf16(tmem, ad, bd, idesc, (jj > 0 || k16 > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(smem_u32(&bar[s]));
+    }
+    last = jj;
+  }
+  if (last >= 0) {
+    if (!mbar_wait_bounded(smem_u32(&bar[last & 1]), (last >> 1) & 1, err, kErrMmaWait)) ok = false;
+  }
+  if (last != nch - 1) ok = false;
+  ok = __syncthreads_and(ok);
+  tc::fence_after_sync();
+  if (ok) {
+    const int m = m0 + warp * 32 + lane;
+    for (int n0 = 0; n0 < np; n0 += 16) {
+      float acc[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + n0, acc);
+      if (m < mtot) {
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+          if (n0 + i < cout) atomicAdd(dw + (size_t)m * cout + n0 + i, acc[i]);
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
+// Weight packing.  w: FP32 master weights in the weight-gradient layout
+// [ntap][cin_p][cout] (row m = t*cin_p + c).  Forward operand
+// B[n = o][k = t*cin_p + c] = w[t][c][o]; data-gradient operand (transposed,
+// taps flipped) B[n = c][k = t*cout_p + o] = w[ntap-1-t][c][o], cout_p = cout
+// rounded up to 8.  Packed layout [kchunks][8][np/8][8 n][8 k], zero outside.
+// ---------------------------------------------------------------------------
+__global__ void pack_weights_kernel(const float *__restrict__ w, int cout, int cin_p, int ntap,
+                                    int transpose, int np, int kchunks, __nv_bfloat16 *out) {
+  const int nout = transpose ? cin_p : cout;                   // GEMM N
+  const int kin = transpose ? ((cout + 7) / 8) * 8 : cin_p;    // channels along K
+  const long long total = (long long)kchunks * kKC * np;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int kk = (int)(e & 7);
+    const int r = (int)((e >> 3) & 7);
+    const long long rest = e >> 6;
+    const int ng = (int)(rest % (np / 8));
+    const long long rest2 = rest / (np / 8);
+    const int kg = (int)(rest2 % 8);
+    const int j = (int)(rest2 / 8);
+    const int n = ng * 8 + r;
+    const int k = j * kKC + kg * 8 + kk;
+    const int t = k / kin, c = k - t * kin;
+    float val = 0.f;
+    if (n < nout && t < ntap) {
+      if (!transpose)
+        val = w[((size_t)t * cin_p + c) * cout + n];
+      else if (c < cout)
+        val = w[((size_t)(ntap - 1 - t) * cin_p + n) * cout + c];
+    }
+    out[e] = __float2bfloat16_rn(val);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Memory-bound pieces.
+// ---------------------------------------------------------------------------
+// 2x2x2 average pooling: out (D/2, H/2, W/2)
+__global__ void avgpool_kernel(View x, int nb, int D, int H, int W, int c, __nv_bfloat16 *y,
+                               int y_cstride, int y_coff) {
+  const int D2 = D / 2, H2 = H / 2, W2 = W / 2, cg = c / 8;
+  const long long total = (long long)nb * D2 * H2 * W2 * cg;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e % cg);
+    long long v = e / cg;
+    const int xx = (int)(v % W2), yy = (int)((v / W2) % H2), zz = (int)((v / ((long long)W2 * H2)) % D2);
+    const int n = (int)(v / ((long long)W2 * H2 * D2));
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int d = 0; d < 8; d++) {
+      const long long vi = (((long long)n * D + 2 * zz + (d >> 2)) * H + 2 * yy + ((d >> 1) & 1)) * W +
+                           2 * xx + (d & 1);
+      const uint4 q = *reinterpret_cast<const uint4 *>(x.p + vi * x.cstride + x.coff + g * 8);
+      const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+      for (int i = 0; i < 8; i++) acc[i] += __bfloat162float(h[i]);
+    }
+    __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = __float2bfloat16_rn(acc[i] * 0.125f);
+    *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff + g * 8) = *reinterpret_cast<const uint4 *>(o);
+  }
+}
+
+// gradient of avgpool: dx (D, H, W) = dy(parent) / 8
+__global__ void avgpool_bwd_kernel(View dy, int nb, int D, int H, int W, int c, __nv_bfloat16 *dx,
+                                   int dx_cstride, int dx_coff, int accumulate) {
+  const int D2 = D / 2, H2 = H / 2, W2 = W / 2, cg = c / 8;
+  const long long total = (long long)nb * D * H * W * cg;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e % cg);
+    const long long v = e / cg;
+    const int xx = (int)(v % W), yy = (int)((v / W) % H), zz = (int)((v / ((long long)W * H)) % D);
+    const int n = (int)(v / ((long long)W * H * D));
+    const long long vp = (((long long)n * D2 + zz / 2) * H2 + yy / 2) * W2 + xx / 2;
+    const uint4 q = *reinterpret_cast<const uint4 *>(dy.p + vp * dy.cstride + dy.coff + g * 8);
+    const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+    __nv_bfloat16 *dst = dx + v * dx_cstride + dx_coff + g * 8;
+    __align__(16) __nv_bfloat16 o[8];
+    const uint4 old = accumulate ? *reinterpret_cast<const uint4 *>(dst) : make_uint4(0, 0, 0, 0);
+    const __nv_bfloat16 *ho = reinterpret_cast<const __nv_bfloat16 *>(&old);
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+      o[i] = __float2bfloat16_rn(__bfloat162float(h[i]) * 0.125f + (accumulate ? __bfloat162float(ho[i]) : 0.f));
+    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(o);
+  }
+}
+
+// nearest upsampling x2: out (2D, 2H, 2W)
+__global__ void upsample_kernel(View x, int nb, int D, int H, int W, int c, __nv_bfloat16 *y,
+                                int y_cstride, int y_coff) {
+  const int cg = c / 8;
+  const int D2 = 2 * D, H2 = 2 * H, W2 = 2 * W;
+  const long long total = (long long)nb * D2 * H2 * W2 * cg;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e % cg);
+    const long long v = e / cg;
+    const int xx = (int)(v % W2), yy = (int)((v / W2) % H2), zz = (int)((v / ((long long)W2 * H2)) % D2);
+    const int n = (int)(v / ((long long)W2 * H2 * D2));
+    const long long vs = (((long long)n * D + zz / 2) * H + yy / 2) * W + xx / 2;
+    *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff + g * 8) =
+        *reinterpret_cast<const uint4 *>(x.p + vs * x.cstride + x.coff + g * 8);
+  }
+}
+
+// gradient of upsampling: dx (D, H, W) = sum of the 8 children
+__global__ void upsample_bwd_kernel(View dy, int nb, int D, int H, int W, int c, __nv_bfloat16 *dx,
+                                    int dx_cstride, int dx_coff) {
+  const int cg = c / 8;
+  const long long total = (long long)nb * D * H * W * cg;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e % cg);
+    const long long v = e / cg;
+    const int xx = (int)(v % W), yy = (int)((v / W) % H), zz = (int)((v / ((long long)W * H)) % D);
+    const int n = (int)(v / ((long long)W * H * D));
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int d = 0; d < 8; d++) {
+      const long long vc = (((long long)n * 2 * D + 2 * zz + (d >> 2)) * 2 * H + 2 * yy + ((d >> 1) & 1)) *
+                               2 * W + 2 * xx + (d & 1);
+      const uint4 q = *reinterpret_cast<const uint4 *>(dy.p + vc * dy.cstride + dy.coff + g * 8);
+      const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+      for (int i = 0; i < 8; i++) acc[i] += __bfloat162float(h[i]);
+    }
+    __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = __float2bfloat16_rn(acc[i]);
+    *reinterpret_cast<uint4 *>(dx + v * dx_cstride + dx_coff + g * 8) = *reinterpret_cast<const uint4 *>(o);
+  }
+}
+
+// dz = dy where y > 0 (ReLU backward), in place on dy's view
+__global__ void relu_mask_kernel(View y, __nv_bfloat16 *dy, int dy_cstride, int dy_coff, long long V,
+                                 int c) {
+  const int cg = c / 8;
+  const long long total = V * cg;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e % cg);
+    const long long v = e / cg;
+    const uint4 qy = *reinterpret_cast<const uint4 *>(y.p + v * y.cstride + y.coff + g * 8);
+    __nv_bfloat16 *dst = dy + v * dy_cstride + dy_coff + g * 8;
+    uint4 qd = *reinterpret_cast<const uint4 *>(dst);
+    const __nv_bfloat16 *hy = reinterpret_cast<const __nv_bfloat16 *>(&qy);
+    __nv_bfloat16 *hd = reinterpret_cast<__nv_bfloat16 *>(&qd);
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+      if (!(__bfloat162float(hy[i]) > 0.f)) hd[i] = __float2bfloat16_rn(0.f);
+    *reinterpret_cast<uint4 *>(dst) = qd;
+  }
+}
+
+// column sums of a BF16 gradient view (the bias gradient): db[c] += sum_v dy[v][c]
+__global__ void bias_grad_kernel(View dy, long long V, int c, float *db) {
+  __shared__ float part[kMaxN];
+  for (int i = threadIdx.x; i < c; i += blockDim.x) part[i] = 0.f;
+  __syncthreads();
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < V * c;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(e % c);
+    const long long v = e / c;
+    atomicAdd(&part[ch], __bfloat162float(dy.p[v * dy.cstride + dy.coff + ch]));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < c; i += blockDim.x) atomicAdd(db + i, part[i]);
+}
+
+// FP32 volume (one channel) -> BF16 channel-last view channel 0, other
+// channels of the 8-channel group zero; scale applied
+__global__ void to_bf16_kernel(const float *in, long long V, float scale, __nv_bfloat16 *y,
+                               int y_cstride, int y_coff) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V;
+       v += (long long)gridDim.x * blockDim.x) {
+    __align__(16) __nv_bfloat16 o[8];
+    o[0] = __float2bfloat16_rn(in[v] * scale);
+#pragma unroll
+    for (int i = 1; i < 8; i++) o[i] = __float2bfloat16_rn(0.f);
+    *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff) = *reinterpret_cast<const uint4 *>(o);
+  }
+}
+
+// loss = mean (out - target)^2; grad (BF16, channel 0 of an 8-channel group) = 2 (out - target) / V
+__global__ void mse_kernel(const float *out, const float *target, long long V, __nv_bfloat16 *g,
+                           int g_cstride, double *loss) {
+  double acc = 0.0;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V;
+       v += (long long)gridDim.x * blockDim.x) {
+    const float r = out[v] - target[v];
+    acc += (double)r * r;
+    __align__(16) __nv_bfloat16 o[8];
+    o[0] = __float2bfloat16_rn(2.f * r / (float)V);
+#pragma unroll
+    for (int i = 1; i < 8; i++) o[i] = __float2bfloat16_rn(0.f);
+    *reinterpret_cast<uint4 *>(g + v * g_cstride) = *reinterpret_cast<const uint4 *>(o);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc / (double)V);
+}
+
+__global__ void adam_kernel(float *p, const float *g, float *m, float *v, long long n, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+static int grid_for(long long n, int threads = 256) {
+  long long g = (n + threads - 1) / threads;
+  return (int)(g < 1 ? 1 : (g > 8 * 152 * 4 ? 8 * 152 * 4 : g));
+}
+
+static size_t conv_smem(int np) {
+  return (size_t)2 * (kTM * kKC * 2 + np * kKC * 2) + 16 + 16 + 128 + kSmemSlack;
+}
+
+}  // namespace sepx
+
+using namespace sepx;
+
+// ---------------------------------------------------------------------------
+// C ABI (include/sepx_unet.h)
+// ---------------------------------------------------------------------------
+namespace {
+int *g_unet_err = nullptr;
+int unet_err_ptr(int **p) {
+  if (!g_unet_err) {
+    if (cudaMalloc((void **)&g_unet_err, sizeof(int)) != cudaSuccess) return -1;
+    if (cudaMemset(g_unet_err, 0, sizeof(int)) != cudaSuccess) return -1;
+  }
+  *p = g_unet_err;
+  return 0;
+}
+int check_conv_args(int cin, int cstride, int coff, int cout, int ntap) {
+  if (cin <= 0 || cin % 8 || cstride % 8 || coff % 8 || coff + cin > cstride) return -1;
+  if (cout <= 0 || cout > kMaxN) return -1;
+  if (ntap != 1 && ntap != 27) return -1;
+  return 0;
+}
+int np_of(int cout) { return ((cout + 15) / 16) * 16; }
+}  // namespace
+
+extern "C" {
+
+int sepx_unet_packed_elems(int cout, int cin_p, int ntap, int transpose) {
+  const int nout = transpose ? cin_p : cout, kin = transpose ? ((cout + 7) / 8) * 8 : cin_p;
+  const int kch = (ntap * kin + kKC - 1) / kKC;
+  return kch * kKC * np_of(nout);
+}
+
+int sepx_unet_pack_weights(const float *w, int cout, int cin_p, int ntap, int transpose, void *out,
+                           void *stream) {
+  const int nout = transpose ? cin_p : cout, kin = transpose ? ((cout + 7) / 8) * 8 : cin_p;
+  if (nout > kMaxN || cin_p % 8 || (ntap != 1 && ntap != 27))
+    return set_error("unet pack: channels (%d -> %d) unsupported", kin, nout);
+  const int np = np_of(nout), kch = (ntap * kin + kKC - 1) / kKC;
+  pack_weights_kernel<<<grid_for((long long)kch * kKC * np), 256, 0, (cudaStream_t)stream>>>(
+      w, cout, cin_p, ntap, transpose, np, kch, (__nv_bfloat16 *)out);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet pack: %s", cudaGetErrorString(e));
+}
+
+int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
+                       int ntap, const void *wpacked, const float *bias, int cout, int relu, void *y,
+                       int y_cstride, int y_coff, float *yf, const float *resid, void *stream) {
+  if (check_conv_args(cin, x_cstride, x_coff, cout, ntap))
+    return set_error("unet conv: bad channel arguments (cin %d cstride %d coff %d cout %d ntap %d)", cin,
+                     x_cstride, x_coff, cout, ntap);
+  if (y && (y_cstride % 8 || y_coff % 8 || cout % 8 || y_coff + cout > y_cstride))
+    return set_error("unet conv: bad output view");
+  int *err;
+  if (unet_err_ptr(&err)) return set_error("unet conv: cannot allocate the status word");
+  const int np = np_of(cout);
+  const int kch = (ntap * cin + kKC - 1) / kKC;
+  const long long V = (long long)nb * D * H * W;
+  const size_t smem = conv_smem(np);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(conv_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)conv_smem(kMaxN));
+    if (e != cudaSuccess) return set_error("unet conv: %s", cudaGetErrorString(e));
+    attr = true;
+  }
+  View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
+  conv_fwd_kernel<<<(unsigned)((V + kTM - 1) / kTM), kUThreads, smem, (cudaStream_t)stream>>>(
+      xv, nb, D, H, W, cin, ntap, (const __nv_bfloat16 *)wpacked, kch, bias, cout, np, relu,
+      (__nv_bfloat16 *)y, y_cstride, y_coff, yf, resid, err);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
+}
+
+int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
+                         int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
+                         float *dw, void *stream) {
+  if (check_conv_args(cin, x_cstride, x_coff, cout, ntap) || dy_cstride % 8 || dy_coff % 8 ||
+      dy_coff + ((cout + 7) / 8) * 8 > dy_cstride)
+    return set_error("unet wgrad: bad channel arguments");
+  int *err;
+  if (unet_err_ptr(&err)) return set_error("unet wgrad: cannot allocate the status word");
+  const int np = np_of(cout);
+  const long long V = (long long)nb * D * H * W;
+  const long long vchunks = (V + kKC - 1) / kKC;
+  const int mt = (ntap * cin + kTM - 1) / kTM;
+  // enough CTAs to fill the GPU about twice, at least 16 voxel chunks each
+  long long per = (vchunks * mt + 2 * 152 * 4 - 1) / (2 * 152 * 4);
+  if (per < 16) per = 16;
+  const long long splits = (vchunks + per - 1) / per;
+  const size_t smem = conv_smem(np);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(conv_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)conv_smem(kMaxN));
+    if (e != cudaSuccess) return set_error("unet wgrad: %s", cudaGetErrorString(e));
+    attr = true;
+  }
+  View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
+  View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  conv_wgrad_kernel<<<dim3(mt, (unsigned)splits), kUThreads, smem, (cudaStream_t)stream>>>(
+      xv, nb, D, H, W, cin, ntap, dv, cout, np, (int)per, dw, err);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet wgrad: %s", cudaGetErrorString(e));
+}
+
+int sepx_unet_avgpool(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int c,
+                      void *y, int y_cstride, int y_coff, void *stream) {
+  if (c % 8 || D % 2 || H % 2 || W % 2) return set_error("unet avgpool: bad shape");
+  View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
+  avgpool_kernel<<<grid_for((long long)nb * D * H * W / 8 * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+      xv, nb, D, H, W, c, (__nv_bfloat16 *)y, y_cstride, y_coff);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet avgpool: launch failed");
+}
+
+int sepx_unet_avgpool_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
+                          int c, void *dx, int dx_cstride, int dx_coff, int accumulate, void *stream) {
+  if (c % 8 || D % 2 || H % 2 || W % 2) return set_error("unet avgpool_bwd: bad shape");
+  View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  avgpool_bwd_kernel<<<grid_for((long long)nb * D * H * W * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+      dv, nb, D, H, W, c, (__nv_bfloat16 *)dx, dx_cstride, dx_coff, accumulate);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet avgpool_bwd: launch failed");
+}
+
+int sepx_unet_upsample(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int c,
+                       void *y, int y_cstride, int y_coff, void *stream) {
+  if (c % 8) return set_error("unet upsample: bad shape");
+  View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
+  upsample_kernel<<<grid_for((long long)nb * D * H * W * 8 * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+      xv, nb, D, H, W, c, (__nv_bfloat16 *)y, y_cstride, y_coff);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet upsample: launch failed");
+}
+
+int sepx_unet_upsample_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
+                           int c, void *dx, int dx_cstride, int dx_coff, void *stream) {
+  if (c % 8) return set_error("unet upsample_bwd: bad shape");
+  View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  upsample_bwd_kernel<<<grid_for((long long)nb * D * H * W * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+      dv, nb, D, H, W, c, (__nv_bfloat16 *)dx, dx_cstride, dx_coff);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet upsample_bwd: launch failed");
+}
+
+int sepx_unet_relu_mask(const void *y, int y_cstride, int y_coff, void *dy, int dy_cstride,
+                        int dy_coff, long long V, int c, void *stream) {
+  if (c % 8) return set_error("unet relu_mask: bad shape");
+  View yv{(const __nv_bfloat16 *)y, y_cstride, y_coff};
+  relu_mask_kernel<<<grid_for(V * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
+      yv, (__nv_bfloat16 *)dy, dy_cstride, dy_coff, V, c);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet relu_mask: launch failed");
+}
+
+int sepx_unet_bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V, int c, float *db,
+                        void *stream) {
+  if (c > kMaxN) return set_error("unet bias_grad: too many channels");
+  View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  bias_grad_kernel<<<grid_for(V * c), 256, 0, (cudaStream_t)stream>>>(dv, V, c, db);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet bias_grad: launch failed");
+}
+
+int sepx_unet_to_bf16(const float *in, long long V, float scale, void *y, int y_cstride, int y_coff,
+                      void *stream) {
+  to_bf16_kernel<<<grid_for(V), 256, 0, (cudaStream_t)stream>>>(in, V, scale, (__nv_bfloat16 *)y,
+                                                                y_cstride, y_coff);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet to_bf16: launch failed");
+}
+
+int sepx_unet_mse(const float *out, const float *target, long long V, void *g, int g_cstride,
+                  double *loss, void *stream) {
+  mse_kernel<<<grid_for(V), 256, 0, (cudaStream_t)stream>>>(out, target, V, (__nv_bfloat16 *)g,
+                                                            g_cstride, loss);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet mse: launch failed");
+}
+
+int sepx_unet_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1,
+                   float b2, float eps, int step, void *stream) {
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet adam: launch failed");
+}
+
+int sepx_unet_status(void) {
+  if (!g_unet_err) return 0;
+  int h = 0;
+  if (cudaMemcpy(&h, g_unet_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return h;
+}
+
+}  // extern "C"

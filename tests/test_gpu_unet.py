@@ -1,0 +1,210 @@
+"""The learned preconditioner's tensor-core kernels against the CPU FP64
+restatement (oracle/unet_oracle.py): convolution forward, data gradient and
+weight gradient per layer shape, the memory-bound pieces, and the gradients of
+the whole network (back-propagation through all 15 layers).
+
+Tolerances: FP32 outputs of a convolution of BF16 operands differ from the
+FP64 sum only by FP32 accumulation order -- relative L2 <= 1e-5.  Outputs
+stored in BF16 carry its rounding (2^-9 relative): <= 8e-3.  Network
+gradients, where BF16 rounding of every activation can flip near a rounding
+boundary and propagate: within 0.1 of the BF16-storage restatement per layer,
+and no further from the exact FP64 gradient than twice that restatement.
+"""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as U
+from tests.harness import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def net():
+    from sep_code_gb300 import unet
+    return unet
+
+
+def _bf(a):
+    return torch.tensor(np.ascontiguousarray(a, np.float32)).to(torch.bfloat16).cuda()
+
+
+def _np(t):
+    return t.float().cpu().numpy().astype(np.float64)
+
+
+def _sync(net):
+    from sep_code_gb300._lib import lib
+    lib.sepx_synchronize()
+    torch.cuda.synchronize()
+
+
+CASES = [(8, 16, 27), (16, 32, 27), (48, 64, 27), (112, 48, 27), (80, 32, 27), (16, 1, 1),
+         (64, 112, 27)]
+
+
+@pytest.mark.parametrize("cin,cout,ntap", CASES)
+def test_conv_forward_dgrad_wgrad(net, cin, cout, ntap):
+    from sep_code_gb300._lib import lib
+    rng = np.random.default_rng(cin * 100 + cout)
+    nb, D, H, W = 2, 8, 16, 16
+    cin_p = (cin + 7) // 8 * 8
+    x = U.bf16(rng.standard_normal((nb, D, H, W, cin_p)))
+    w = (rng.standard_normal((ntap, cin_p, cout)) / np.sqrt(ntap * cin)).astype(np.float32)
+    b = rng.standard_normal(cout).astype(np.float32)
+    lib.sepx_setup_cuda(1)
+    st = lib.sepx_get_stream()
+    wt = torch.tensor(w, dtype=torch.float32).cuda()
+    bt = torch.tensor(b, dtype=torch.float32).cuda()
+    pk = torch.zeros(net.lib.sepx_unet_packed_elems(cout, cin_p, ntap, 0), dtype=torch.bfloat16).cuda()
+    pkt = torch.zeros(net.lib.sepx_unet_packed_elems(cout, cin_p, ntap, 1), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_pack_weights(net._p(wt), cout, cin_p, ntap, 0, net._p(pk), st))
+    net._chk(net.lib.sepx_unet_pack_weights(net._p(wt), cout, cin_p, ntap, 1, net._p(pkt), st))
+    xt = _bf(x)
+    V = nb * D * H * W
+    yf = torch.zeros(V * cout, dtype=torch.float32).cuda()
+    torch.cuda.synchronize()
+    # forward, FP32 output
+    net._chk(net.lib.sepx_unet_conv_fwd(net._p(xt), cin_p, 0, nb, D, H, W, cin_p, ntap, net._p(pk),
+                                        net._p(bt), cout, 0, None, 0, 0, net._p(yf), None, st))
+    _sync(net)
+    want = U.conv_fwd(x, U.bf16(w), b, False)
+    got = yf.cpu().numpy().reshape(want.shape)
+    assert net.lib.sepx_unet_status() == 0
+    assert rel_l2(got, want) <= 1e-5, rel_l2(got, want)
+    # forward with ReLU into a BF16 channel slice of a wider buffer
+    if cout % 8 == 0:
+        ybuf = torch.zeros((V, cout + 16), dtype=torch.bfloat16).cuda()
+        torch.cuda.synchronize()
+        net._chk(net.lib.sepx_unet_conv_fwd(net._p(xt), cin_p, 0, nb, D, H, W, cin_p, ntap, net._p(pk),
+                                            net._p(bt), cout, 1, net._p(ybuf), cout + 16, 8, None,
+                                            None, st))
+        _sync(net)
+        yb = _np(ybuf)
+        assert rel_l2(yb[:, 8:8 + cout].reshape(want.shape), np.maximum(want, 0)) <= 8e-3
+        assert not yb[:, :8].any() and not yb[:, 8 + cout:].any()
+    # data gradient: dx = conv^T(dy), BF16 output
+    cout_p = (cout + 7) // 8 * 8
+    dy = np.zeros((nb, D, H, W, cout_p))
+    dy[..., :cout] = U.bf16(rng.standard_normal((nb, D, H, W, cout)))
+    dyt = _bf(dy)
+    dx = torch.zeros((V, cin_p), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_conv_fwd(net._p(dyt), cout_p, 0, nb, D, H, W, cout_p, ntap, net._p(pkt),
+                                        None, cin_p, 0, net._p(dx), cin_p, 0, None, None, st))
+    _sync(net)
+    want_dx = U.conv_dgrad(dy[..., :cout], U.bf16(w))
+    assert rel_l2(_np(dx).reshape(want_dx.shape), want_dx) <= 8e-3
+    # weight gradient, FP32 accumulation (added to what dw holds)
+    dw = torch.full((ntap * cin_p * cout,), 0.25, dtype=torch.float32).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_conv_wgrad(net._p(xt), cin_p, 0, nb, D, H, W, cin_p, ntap, net._p(dyt),
+                                          cout_p, 0, cout, net._p(dw), st))
+    _sync(net)
+    want_dw = U.conv_wgrad(x, dy[..., :cout], ntap, cin_p) + 0.25
+    assert rel_l2(dw.cpu().numpy().reshape(want_dw.shape), want_dw) <= 1e-5
+    assert net.lib.sepx_unet_status() == 0
+
+
+def test_pool_upsample_mask(net):
+    from sep_code_gb300._lib import lib
+    lib.sepx_setup_cuda(1)
+    st = lib.sepx_get_stream()
+    rng = np.random.default_rng(3)
+    nb, D, H, W, C = 2, 8, 8, 16, 16
+    x = U.bf16(rng.standard_normal((nb, D, H, W, C)))
+    xt = _bf(x)
+    V = nb * D * H * W
+    y = torch.zeros((V // 8, C), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_avgpool(net._p(xt), C, 0, nb, D, H, W, C, net._p(y), C, 0, st))
+    _sync(net)
+    assert rel_l2(_np(y), U.bf16(U.avgpool(x)).reshape(-1, C)) <= 1e-6
+    up = torch.zeros((V, C), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_upsample(net._p(y), C, 0, nb, D // 2, H // 2, W // 2, C, net._p(up), C,
+                                        0, st))
+    _sync(net)
+    assert np.array_equal(_np(up), U.upsample(_np(y).reshape(nb, D // 2, H // 2, W // 2, C)).reshape(-1, C))
+    ub = torch.zeros((V // 8, C), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_upsample_bwd(net._p(xt), C, 0, nb, D // 2, H // 2, W // 2, C, net._p(ub),
+                                            C, 0, st))
+    _sync(net)
+    assert rel_l2(_np(ub), U.bf16(U.upsample_bwd(x)).reshape(-1, C)) <= 1e-6
+    m = _bf(x)
+    g = _bf(np.ones_like(x))
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_relu_mask(net._p(m), C, 0, net._p(g), C, 0, V, C, st))
+    _sync(net)
+    assert np.array_equal(_np(g).reshape(x.shape), (x > 0).astype(np.float64))
+
+
+def test_network_gradients_match_oracle(net):
+    """one forward + backward of the whole U-Net on a 32^3 volume (4^3 at the
+    bottom level), every layer's weight and bias gradient against the FP64
+    restatement.  The GPU rounds every stored activation and gradient to BF16
+    after FP32 sums, the restatement after FP64 sums: where the two roundings
+    differ (or a ReLU input sits within a rounding of zero) the difference
+    propagates, most at the coarse levels whose sums have fewest terms.  A
+    wiring error (a wrong channel slice, skip or pooling gradient) shows as
+    an O(1) error instead."""
+    rng = np.random.default_rng(11)
+    params = net.init_params(seed=5)
+    w, b = params["out"]
+    params["out"] = (rng.standard_normal(w.shape).astype(np.float32) * 0.3, b + 0.01)
+    params = {k: (v[0], v[1] + rng.standard_normal(v[1].shape).astype(np.float32) * 0.05)
+              for k, v in params.items()}
+    nb, D, H, W = 1, 32, 32, 32
+    x = rng.standard_normal((nb, D, H, W)).astype(np.float32)
+    tgt = rng.standard_normal((nb, D, H, W)).astype(np.float32)
+    model = net.UNet3D(params)
+    xt = torch.tensor(x).cuda()
+    tt = torch.tensor(tgt).cuda()
+    torch.cuda.synchronize()
+    model.zero_grad()
+    out = model.forward_device(xt)
+    model.loss_grad(tt)
+    model.backward_device()
+    model.stream.synchronize()
+    assert model.status() == 0
+    o_out, o_loss, o_g = U.forward_backward(params, x, tgt)
+    _, _, ex_g = U.forward_backward(params, x, tgt, round_bf16=False)
+    # BF16 activations through 15 layers: a rounding that flips between the
+    # FP32 and the FP64 sums moves the output at the 1e-3 level
+    assert rel_l2(out.cpu().numpy().reshape(o_out.shape), o_out) <= 1e-2
+    assert abs(float(model.loss.item()) - o_loss) <= 1e-2 * o_loss
+    errs = {}
+    for L in net.LAYERS:
+        gw = model.gw[L.name].cpu().numpy()
+        gb = model.gb[L.name].cpu().numpy()
+        ew, eb = o_g[L.name]
+        xw, xb = ex_g[L.name]
+        assert np.abs(ew).max() > 0, L.name
+        # against the BF16-storage restatement, and how far the GPU and that
+        # restatement each sit from the exact FP64 gradient
+        errs[L.name] = (rel_l2(gw, ew), rel_l2(gb, eb), rel_l2(gw, xw), rel_l2(ew, xw))
+    print("UNET_GRAD_REL_L2", errs)
+    for name, (ew_, eb_, gx, ox) in errs.items():
+        assert ew_ <= 0.1 and eb_ <= 0.1, (name, ew_, eb_)
+        assert gx <= 2.0 * ox + 0.01, (name, gx, ox)
+
+
+def test_training_reduces_loss(net):
+    """Adam on a fixed smoothing task: the loss falls by more than half"""
+    rng = np.random.default_rng(2)
+    model = net.UNet3D(seed=1)
+    nb, D, H, W = 2, 16, 16, 16
+    x = rng.standard_normal((nb, D, H, W)).astype(np.float32)
+    # target: 3-point smoothing along every axis of x (a fixed linear operator)
+    t = x.copy()
+    for ax in (1, 2, 3):
+        t = (np.roll(t, 1, ax) + 2 * t + np.roll(t, -1, ax)) / 4
+    xt, tt = torch.tensor(x).cuda(), torch.tensor(t.astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    losses = [model.train_step(xt, tt, lr=2e-3) for _ in range(60)]
+    assert model.status() == 0
+    assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
