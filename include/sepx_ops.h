@@ -58,9 +58,13 @@ int sepx_rtm_op_dot_test(sepx_op_handle op, unsigned long long seed, double out[
  * :115-143; Born/cgstep.cpp:14-58): niter iterations from m = 0; writes the
  * model, the FP64 residual energy rr.rr after each iteration and the wall
  * seconds at each iteration; `dir` (may be NULL) preconditions the search
- * direction g before the forward product. */
+ * direction g before the forward product.  fallback_ratio > 0: once a
+ * preconditioned iteration leaves rr.rr above fallback_ratio times its
+ * previous value, the remaining iterations use plain g (the iteration is
+ * written to *fallback_iter, -1 if none; may be NULL). */
 int sepx_lsrtm(sepx_op_handle op, const float *data, int niter, float *model, double *resid,
-               double *seconds, sepx_direction_fn dir, void *dir_ctx);
+               double *seconds, sepx_direction_fn dir, void *dir_ctx, double fallback_ratio,
+               int *fallback_iter);
 
 #ifdef __cplusplus
 }
@@ -217,6 +221,8 @@ class lin_solver {
   // optional preconditioning of the search direction before forward(g, gg)
   sepx_direction_fn dir = nullptr;
   void *dir_ctx = nullptr;
+  double fallback_ratio = 0.0;   // > 0: switch to plain g once a step gains less
+  int fallback_iter = -1;
   std::vector<double> resid, seconds;
   my_vector *g = nullptr, *m = nullptr, *gg = nullptr, *rr = nullptr;
   my_operator *oper = nullptr;

@@ -336,9 +336,11 @@ my_vector *lin_solver::init_rr(my_vector *data, my_operator *op, my_vector *m0) 
 }
 bool lin_solver::solve(int niter) {
   const auto t0 = std::chrono::steady_clock::now();
+  double prev = rr->dot(rr);
+  bool use_dir = dir != nullptr;
   for (int iter = 0; iter < niter; iter++) {
     oper->adjoint(false, g, rr, iter);
-    if (dir) {
+    if (use_dir) {
       auto *gh = dynamic_cast<hypercube_float *>(g);
       if (!gh) throw std::runtime_error("direction preconditioning needs a hypercube_float model");
       ck(dir(dir_ctx, gh->vals, gh->n123), "direction preconditioner");
@@ -347,6 +349,13 @@ bool lin_solver::solve(int niter) {
     double val = 0;
     const bool valid = st->step_it(iter, m, g, rr, gg, &val);
     if (!valid) return false;
+    // plain CG is the fallback: once a preconditioned step lowers rr.rr by
+    // less than the ratio allows, the remaining iterations use plain g
+    if (use_dir && fallback_ratio > 0 && val > fallback_ratio * prev) {
+      use_dir = false;
+      fallback_iter = iter;
+    }
+    prev = val;
     resid.push_back(val);
     seconds.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
     if (verb > 0) fprintf(stderr, "iter %d residual %g\n", iter, val);
@@ -645,7 +654,8 @@ int sepx_rtm_op_dot_test(sepx_op_handle h, unsigned long long seed, double out[4
 }
 
 int sepx_lsrtm(sepx_op_handle h, const float *data, int niter, float *model, double *resid,
-               double *seconds, sepx_direction_fn dir, void *dir_ctx) {
+               double *seconds, sepx_direction_fn dir, void *dir_ctx, double fallback_ratio,
+               int *fallback_iter) {
   try {
     auto *b = static_cast<op_box *>(h);
     b->data->upload(data);
@@ -653,7 +663,9 @@ int sepx_lsrtm(sepx_op_handle h, const float *data, int niter, float *model, dou
     simple_solver solv(&st, b->data.get(), b->op.get());
     solv.dir = dir;
     solv.dir_ctx = dir_ctx;
+    solv.fallback_ratio = fallback_ratio;
     solv.solve(niter);
+    if (fallback_iter) *fallback_iter = solv.fallback_iter;
     std::unique_ptr<my_vector> mod(solv.return_model());
     hf(mod.get())->download(model);
     for (size_t i = 0; i < solv.resid.size(); i++) {

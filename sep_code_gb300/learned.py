@@ -190,7 +190,7 @@ def lsrtm_survey(n: int = 384, nt: int = 3000, nshots: int = 4, d: float = 12.5,
 
 
 def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 4,
-                  snap_prec: str = "bf16", verbose: bool = False) -> dict:
+                  snap_prec: str = "bf16", fallback_ratio: float = 0.9, verbose: bool = False) -> dict:
     """Plain simple_solver + cgstep against the same solver with the learned
     direction, on data d = L m_true of the survey's reflectivity."""
     op = RtmOperator(s, mode="linear", snap_js=snap_js, snap_prec=snap_prec)
@@ -204,7 +204,8 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
             print("plain", np.sqrt(r_plain / dd), s_plain, flush=True)
         net = load_network() if net is None else net
         hook = UNetDirection(net, op.model_shape)
-        m_nn, r_nn, s_nn = op.lsrtm(d, niter, direction=hook)
+        m_nn, r_nn, s_nn = op.lsrtm(d, niter, direction=hook, fallback_ratio=fallback_ratio)
+        fb_iter = op.fallback_iter
         if verbose:
             print("learned", np.sqrt(r_nn / dd), s_nn, flush=True)
     finally:
@@ -224,7 +225,8 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
         "seconds_data_generation": t_fwd,
         "plain": {"rel_residual": rp.tolist(), "seconds": s_plain.tolist()},
         "learned": {"rel_residual": rn.tolist(), "seconds": s_nn.tolist(),
-                    "direction_seconds": hook.seconds},
+                    "direction_seconds": hook.seconds, "direction_calls": hook.calls,
+                    "fallback_ratio": fallback_ratio, "plain_g_from_iteration": fb_iter + 1 if fb_iter >= 0 else None},
         "time_to_1e-2": {"plain": t_to(rp, s_plain, 1e-2), "learned": t_to(rn, s_nn, 1e-2)},
         "time_to_plain_final_residual": {"plain": float(s_plain[-1]),
                                          "learned": t_to(rn, s_nn, final_plain)},

@@ -39,7 +39,8 @@ lib.sepx_rtm_op_data_size.restype = C.c_longlong
 lib.sepx_rtm_op_forward.argtypes = [C.c_void_p, C.c_int, _F32P, _F32P]
 lib.sepx_rtm_op_adjoint.argtypes = [C.c_void_p, C.c_int, _F32P, _F32P]
 lib.sepx_rtm_op_dot_test.argtypes = [C.c_void_p, C.c_ulonglong, _F64P]
-lib.sepx_lsrtm.argtypes = [C.c_void_p, _F32P, C.c_int, _F32P, _F64P, _F64P, C.c_void_p, C.c_void_p]
+lib.sepx_lsrtm.argtypes = [C.c_void_p, _F32P, C.c_int, _F32P, _F64P, _F64P, C.c_void_p, C.c_void_p,
+                           C.c_double, C.POINTER(C.c_int)]
 
 MODES = {"reference": 0, "linear": 1}
 PREC = {"f32": 0, "bf16": 1, "f16": 2}
@@ -95,16 +96,21 @@ class RtmOperator:
         self._chk(lib.sepx_rtm_op_dot_test(self.h, seed, out))
         return out
 
-    def lsrtm(self, data, niter: int, direction=None):
+    def lsrtm(self, data, niter: int, direction=None, fallback_ratio: float = 0.0):
         """simple_solver + cgstep; ``direction(g_ptr, n)`` may precondition the
-        search direction in place (device pointer).  Returns (model, rr.rr per
-        iteration, seconds per iteration)."""
+        search direction in place (device pointer); with fallback_ratio > 0 the
+        solver returns to plain g once a preconditioned step lowers rr.rr by
+        less than that ratio (``self.fallback_iter`` records where).  Returns
+        (model, rr.rr per iteration, seconds per iteration)."""
         model = np.zeros(self.model_shape, np.float32)
         resid = np.zeros(niter, np.float64)
         secs = np.zeros(niter, np.float64)
         cb = None
         if direction is not None:
             cb = DIRECTION_FN(lambda ctx, g, n: int(direction(g, n) or 0))
+        fb = C.c_int(-1)
         self._chk(lib.sepx_lsrtm(self.h, np.ascontiguousarray(data, np.float32), niter, model, resid, secs,
-                                 C.cast(cb, C.c_void_p) if cb else None, None))
+                                 C.cast(cb, C.c_void_p) if cb else None, None, fallback_ratio,
+                                 C.byref(fb)))
+        self.fallback_iter = fb.value
         return model, resid, secs
