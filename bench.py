@@ -44,6 +44,9 @@ def parse_args():
     p.add_argument("--cpu-sample-steps", type=int, default=10)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", default="rtm", choices=["rtm", "batch"],
+                   help="rtm: the single-shot RTM line; batch: 16 batched shots")
+    p.add_argument("--batch-nt", type=int, default=1000)
     return p.parse_args()
 
 
@@ -379,6 +382,51 @@ def run_ours(args, ws, rank, dist):
         print(json.dumps(out))
 
 
+# ------------------------------------------------------------------ batched shots
+def run_batch(args):
+    """16 uneven-window shots on a 1024 x 1024 x 400 model: the Born forward
+    of every shot, shot after shot (the reference's shot loop) against one
+    persistent launch per step, with and without a captured CUDA graph, after
+    the autotuner picked the z-chunk and ring depth."""
+    import torch
+    from sep_code_gb300 import batch as Bt
+    nt = args.batch_nt
+    t0 = time.perf_counter()
+    surveys = Bt.config4_surveys(nt=nt)
+    b = Bt.BatchRTM(surveys)
+    t_setup = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(Bt.lib.sepx_get_stream())
+    updates = b.cell_updates()
+    out = {"metric": "Gcell-updates/s (batched Born forward, 16 shots)", "unit": "Gcell/s",
+           "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "batch_16_shots_1024x1024x400", "nt": nt,
+                      "windows": [list(s.vel.shape[::-1]) for s in surveys],
+                      "padded": ["x".join(map(str, st.n)) for st in b.setups],
+                      "cells_per_step": int(sum(b.cells))},
+           "setup_seconds": round(t_setup, 1)}
+    z, st_, sty, ms = b.autotune(nsteps=8)
+    out["autotune"] = {"zchunk": z, "stages": st_, "style": ["all-tiles", "persistent"][sty],
+                       "ms_per_step": round(ms, 4)}
+    res = {}
+    for how in ("sequential", "persistent", "graph", "graph"):
+        b.zero_traces()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.forward(how)
+        e1.record(stream)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        key = how if how not in res else how + "_replay"
+        res[key] = {"seconds": round(sec, 4), "gcells": round(updates / sec / 1e9, 2)}
+    b.close()
+    out["runs"] = res
+    out["value"] = res["graph_replay"]["gcells"]
+    out["speedup_vs_sequential"] = round(res["sequential"]["seconds"] / res["graph_replay"]["seconds"], 3)
+    print(json.dumps(out))
+
+
 # ------------------------------------------------------------------ reference arm
 def run_reference(args, ws, rank):
     """The reference has no CPU propagation; its CPU path is the oracle's
@@ -419,7 +467,10 @@ def main():
     args = parse_args()
     ws, rank, local = dist_env()
     dist = dist_init(ws, local)
-    if args.impl == "reference":
+    if args.workload == "batch" and args.impl == "ours":
+        if rank == 0:
+            run_batch(args)
+    elif args.impl == "reference":
         run_reference(args, ws, rank)
     else:
         run_ours(args, ws, rank, dist)

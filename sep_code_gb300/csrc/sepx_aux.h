@@ -8,6 +8,12 @@ namespace sepx {
 
 cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st);
 size_t prop_smem_bytes(int mode);
+// persistent multi-grid launches (sepx_prop.cu): stages 3 or 4
+bool batch_supported(int mode, int stages);
+cudaError_t launch_prop_batch(int mode, int stages, const PropParams *params, const int4 *items,
+                              int nitems, const BatchStep &step, int grid, cudaStream_t st);
+int prop_batch_occupancy(int mode, int stages);   // resident CTAs per SM
+cudaError_t launch_prop_multi(int mode, int stages, const MultiParams &mp, cudaStream_t st);
 
 cudaError_t launch_inj_values(const float *src, int ntrace, int npts, const float *sinc, int nsinc,
                               int jt, int nsteps, int j0, float dir, float *out, cudaStream_t st);

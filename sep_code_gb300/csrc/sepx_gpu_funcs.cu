@@ -12,6 +12,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -21,6 +22,7 @@
 #include <vector>
 
 #include "../../include/sepx.h"
+#include "../../include/sepx_batch.h"
 #include "sepx_aux.h"
 #include "sepx_blas.h"
 #include "sepx_common.h"
@@ -52,10 +54,8 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   int *d_err = nullptr;
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  long long launches = 0;
   int zchunk_override = 0;
   int num_sms = 152;
-  std::string err;
   // grid
   bool have_grid = false;
   int n1 = 0, n2 = 0, n3 = 0, pitch = 0;
@@ -101,7 +101,13 @@ struct Ctx {
   int snap_js = 0, snap_prec = -1, snap_nt = -1;
 };
 
-Ctx G;
+// The current context.  One shot lives in one context; a batch of shots
+// (sepx_batch_*) holds one context per shot and switches between them.
+Ctx g_default;
+Ctx *g_cur = &g_default;
+#define G (*g_cur)
+std::string g_err;          // the last error message, whichever context raised it
+long long g_launches = 0;   // kernels launched through this library
 
 int fail(const char *fmt, ...) {
   char buf[1024];
@@ -109,7 +115,7 @@ int fail(const char *fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  G.err = buf;
+  g_err = buf;
   return -1;
 }
 
@@ -123,7 +129,7 @@ int fail(const char *fmt, ...) {
 #define CKL(expr)                                                                        \
   do {                                                                                   \
     cudaError_t e_ = (expr);                                                             \
-    G.launches++;                                                                        \
+    g_launches++;                                                                        \
     if (e_ != cudaSuccess)                                                               \
       return fail("kernel launch %s failed: %s", #expr, cudaGetErrorString(e_));         \
   } while (0)
@@ -614,7 +620,7 @@ int set_error(const char *fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  G.err = buf;
+  g_err = buf;
   return -1;
 }
 
@@ -1034,7 +1040,7 @@ int sepx_synchronize(void) {
   return check_device_error();
 }
 
-const char *sepx_last_error(void) { return G.err.c_str(); }
+const char *sepx_last_error(void) { return g_err.c_str(); }
 
 int sepx_device_error(void) {
   if (!G.have_device) return 0;
@@ -1044,7 +1050,7 @@ int sepx_device_error(void) {
   return h;
 }
 
-long long sepx_kernel_launches(void) { return G.launches; }
+long long sepx_kernel_launches(void) { return g_launches; }
 
 int sepx_set_zchunk(int planes) {
   if (planes < 0) return fail("zchunk must be >= 0");
@@ -1064,7 +1070,7 @@ int sepx_reset(void) {
 
 // ------------------------------------------------------------ reference-named ABI
 static void report(int rc, const char *who) {
-  if (rc) fprintf(stderr, "sepx: %s: %s\n", who, G.err.c_str());
+  if (rc) fprintf(stderr, "sepx: %s: %s\n", who, g_err.c_str());
 }
 
 void setup_cuda(int ngpus, int argc, char **argv) {
@@ -1107,3 +1113,6 @@ void rtm_adjoint(int n1, int n2, int n3, int j, float *p0_s_cpu, float *p1_s_cpu
 }
 
 }  // extern "C"
+
+// Batches of shots: one context per shot, one persistent launch per step.
+#include "sepx_batch.inc"

@@ -227,14 +227,27 @@ __device__ __forceinline__ float4 mul4(float4 a, float4 b) {
                      __fmul_rn(a.w, b.w));
 }
 
+// Shared-memory carve of one CTA: [STAGES stages][full bars][empty bars]
+// [4-float block max][sponge table] from a 128-byte aligned base.
 template <int MODE, int STAGES>
-__global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(const __grid_constant__ PropParams P) {
+__device__ __forceinline__ float *smem_base(unsigned char *raw) {
+  return reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(raw) + 127) &
+                                   ~static_cast<uintptr_t>(127));
+}
+template <int MODE, int STAGES>
+__host__ __device__ constexpr size_t smem_carve_bytes() {
+  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 16 + 4 * kTabSmem;
+}
+
+// One tile (32 x 16 cells, z-chunk bz) of one fused step.  P holds the
+// parameters the step reads; T the tensor maps (param or global memory: TMA
+// cannot read them from shared memory).  Leaves the CTA with no copy in
+// flight and its barriers invalidated, so that the next tile may start.
+template <int MODE, int STAGES>
+__device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &T, int bx, int by,
+                                         int bz, float *smem) {
   using M = Mode<MODE>;
   constexpr int NF = M::NF;
-  // dynamic shared memory only: [<=127 B pad][STAGES stages][full bars][empty bars]
-  extern __shared__ unsigned char smem_raw[];
-  float *smem = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
-                                          ~static_cast<uintptr_t>(127));
   unsigned long long *bar_full = reinterpret_cast<unsigned long long *>(smem + STAGES * M::STAGE);
   unsigned long long *bar_empty = bar_full + STAGES;
   float *red = reinterpret_cast<float *>(bar_empty + STAGES);   // 4 floats: block max
@@ -243,9 +256,9 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(c
   const PropGeom &g = P.g;
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int x0 = g.xb + kTX * blockIdx.x;
-  const int y0 = g.yb + kTY * blockIdx.y;
-  const int za = g.zb + g.zchunk * blockIdx.z;
+  const int x0 = g.xb + kTX * bx;
+  const int y0 = g.yb + kTY * by;
+  const int za = g.zb + g.zchunk * bz;
   const int niter = min(g.zchunk, g.ze - za);
   if (niter <= 0) return;   // uniform for the CTA
 
@@ -267,9 +280,9 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(c
     // ---------------- producer ----------------
     if (lane == 0) {
       for (int f = 0; f < NF; f++) {
-        prefetch_tmap(&P.tm_cur_h[f]);
-        prefetch_tmap(&P.tm_cur_c[f]);
-        prefetch_tmap(&P.tm_prev_c[f]);
+        prefetch_tmap(&T.tm_cur_h[f]);
+        prefetch_tmap(&T.tm_cur_c[f]);
+        prefetch_tmap(&T.tm_prev_c[f]);
       }
       for (int i = 0; i < niter; i++) {
         const int s = i % STAGES;
@@ -283,19 +296,19 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(c
         float *st = smem + s * M::STAGE;
         const int z = za + i;
         for (int f = 0; f < NF; f++)
-          tma_load_3d(smem_u32(st + M::FEED + f * kCenterFloats), &P.tm_cur_c[f], x0, y0, z + 4, fb);
-        if (M::VEL_HALO) tma_load_3d(smem_u32(st + M::FEEDV), &P.tm_vel_c, x0, y0, z + 4, fb);
+          tma_load_3d(smem_u32(st + M::FEED + f * kCenterFloats), &T.tm_cur_c[f], x0, y0, z + 4, fb);
+        if (M::VEL_HALO) tma_load_3d(smem_u32(st + M::FEEDV), &T.tm_vel_c, x0, y0, z + 4, fb);
         for (int f = 0; f < NF; f++)
-          tma_load_3d(smem_u32(st + M::HALO + f * kHaloFloats), &P.tm_cur_h[f], x0 - kHalo,
+          tma_load_3d(smem_u32(st + M::HALO + f * kHaloFloats), &T.tm_cur_h[f], x0 - kHalo,
                       y0 - kHalo, z, fb);
         if (M::VEL_HALO)
-          tma_load_3d(smem_u32(st + M::VELT), &P.tm_vel_h, x0 - kHalo, y0 - kHalo, z, fb);
+          tma_load_3d(smem_u32(st + M::VELT), &T.tm_vel_h, x0 - kHalo, y0 - kHalo, z, fb);
         else
-          tma_load_3d(smem_u32(st + M::VELT), &P.tm_vel_c, x0, y0, z, fb);
+          tma_load_3d(smem_u32(st + M::VELT), &T.tm_vel_c, x0, y0, z, fb);
         for (int f = 0; f < NF; f++)
-          tma_load_3d(smem_u32(st + M::PREV + f * kCenterFloats), &P.tm_prev_c[f], x0, y0, z, fb);
-        if (load_img) tma_load_3d(smem_u32(st + M::IMG), &P.tm_img_c, x0, y0, z, fb);
-        if (M::HAS_AUX) tma_load_3d(smem_u32(st + M::AUX), &P.tm_aux_c, x0, y0, z, fb);
+          tma_load_3d(smem_u32(st + M::PREV + f * kCenterFloats), &T.tm_prev_c[f], x0, y0, z, fb);
+        if (load_img) tma_load_3d(smem_u32(st + M::IMG), &T.tm_img_c, x0, y0, z, fb);
+        if (M::HAS_AUX) tma_load_3d(smem_u32(st + M::AUX), &T.tm_aux_c, x0, y0, z, fb);
         issued = i + 1;
       }
     }
@@ -469,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(c
       long long blk = 0, eoff = 0;
       if (M::LIN) {
         const int ntx = (g.xe - g.xb + kTX - 1) / kTX, nty = (g.ye - g.yb) / kTY;
-        blk = ((P.snap_index * (g.ze - g.zb) + (z - g.zb)) * nty + blockIdx.y) * ntx + blockIdx.x;
+        blk = ((P.snap_index * (g.ze - g.zb) + (z - g.zb)) * nty + by) * ntx + bx;
         eoff = blk * kCenterFloats + row * kTX + 4 * xq;
       }
       if ((MODE == kLinSrc || MODE == kLinFwd) && P.do_snap && P.snap_prec != kSnapF32) {
@@ -614,11 +627,85 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB) prop_step_kernel(c
         break;
     }
   }
+  __syncthreads();
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_inval(smem_u32(&bar_full[s]));
+      mbar_inval(smem_u32(&bar_empty[s]));
+    }
+  }
+}
+
+template <int MODE, int STAGES>
+__global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB)
+    prop_step_kernel(const __grid_constant__ PropParams P) {
+  extern __shared__ unsigned char smem_raw[];
+  run_tile<MODE, STAGES>(P, P, blockIdx.x, blockIdx.y, blockIdx.z, smem_base<MODE, STAGES>(smem_raw));
+}
+
+// Many shots (or any set of grids) in one persistent launch: CTA b runs the
+// tiles b, b + gridDim.x, ... of the item list.  Item = (shot, tile x, tile
+// y, z-chunk), parameter set 2*shot + the step's parity; the parameter set's scalars are copied into shared
+// memory and the step's values patched in (injection row, trace sample,
+// sinc row, scattering / imaging switches), its tensor maps read from global
+// memory.
+// The batched kernel reads its scalars from shared memory (the single-launch
+// kernel reads them as constant operands), so the two-field modes get the
+// register budget of 2 CTAs per SM.
+template <int MODE>
+constexpr int batch_minb() {
+  return (MODE == kBornFwd || MODE == kRtmAdj) ? 2 : Mode<MODE>::MINB;
+}
+
+template <int MODE, int STAGES>
+__global__ void __launch_bounds__(kThreads, batch_minb<MODE>())
+    prop_batch_kernel(const PropParams *__restrict__ params, const int4 *__restrict__ items,
+                      int nitems, BatchStep step) {
+  extern __shared__ unsigned char smem_raw[];
+  float *smem = smem_base<MODE, STAGES>(smem_raw);
+  PropParams *Ps = reinterpret_cast<PropParams *>(
+      reinterpret_cast<unsigned char *>(smem) + ((smem_carve_bytes<MODE, STAGES>() + 63) & ~size_t(63)));
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 item = items[it];
+    const PropParams *Pg = params + 2 * item.x + step.parity;
+    const uint4 *src = reinterpret_cast<const uint4 *>(Pg);
+    uint4 *dst = reinterpret_cast<uint4 *>(Ps);
+    for (int i = threadIdx.x; i < (int)(sizeof(PropParams) / 16); i += kThreads) dst[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      Ps->inj_s = Pg->inj_s + (long long)step.inj_row * Pg->inj_stride;
+      Ps->trc_id = step.trc_id;
+      Ps->sinc_row = Pg->sinc_row + step.sinc_ii * 8;
+      Ps->do_scatter = step.do_scatter;
+      Ps->do_image = step.do_image;
+    }
+    __syncthreads();
+    run_tile<MODE, STAGES>(*Ps, *Pg, item.y, item.z, item.w, smem);
+    __syncthreads();
+  }
+}
+
+// Up to kMaxMulti grids in one launch, parameters in parameter space.
+template <int MODE, int STAGES>
+__global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB)
+    prop_multi_kernel(const __grid_constant__ MultiParams mp) {
+  extern __shared__ unsigned char smem_raw[];
+  const int b = blockIdx.x;
+  int s = 0;
+  while (s + 1 < mp.nshot && b >= mp.tile_base[s + 1]) s++;
+  const int local = b - mp.tile_base[s];
+  const int ntx = mp.ntx[s], nty = mp.nty[s];
+  const int bx = local % ntx, by = (local / ntx) % nty, bz = local / (ntx * nty);
+  run_tile<MODE, STAGES>(mp.p[s], mp.p[s], bx, by, bz, smem_base<MODE, STAGES>(smem_raw));
 }
 
 template <int MODE, int STAGES>
 constexpr size_t smem_bytes_of() {
-  return (size_t)STAGES * Mode<MODE>::STAGE * 4 + 2 * STAGES * 8 + 16 + 4 * kTabSmem + 128;
+  return smem_carve_bytes<MODE, STAGES>() + 128;
+}
+template <int MODE, int STAGES>
+constexpr size_t batch_smem_bytes_of() {
+  return ((smem_carve_bytes<MODE, STAGES>() + 63) & ~size_t(63)) + sizeof(PropParams) + 128;
 }
 
 template <int MODE, int STAGES>
@@ -651,6 +738,82 @@ cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
     case kLinAdj: return launch_mode<kLinAdj, 3>(P, grid, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// ---- batched launches ----
+template <int MODE, int STAGES>
+static cudaError_t launch_multi_mode(const MultiParams &mp, cudaStream_t st) {
+  const size_t smem = smem_bytes_of<MODE, STAGES>();
+  auto kern = prop_multi_kernel<MODE, STAGES>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  const int ntiles = mp.tile_base[mp.nshot];
+  if (ntiles <= 0) return cudaSuccess;
+  kern<<<ntiles, kThreads, smem, st>>>(mp);
+  return cudaGetLastError();
+}
+
+template <int MODE, int STAGES>
+static cudaError_t launch_batch_mode(const PropParams *params, const int4 *items, int nitems,
+                                     const BatchStep &step, int grid, cudaStream_t st) {
+  const size_t smem = batch_smem_bytes_of<MODE, STAGES>();
+  auto kern = prop_batch_kernel<MODE, STAGES>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  kern<<<grid, kThreads, smem, st>>>(params, items, nitems, step);
+  return cudaGetLastError();
+}
+
+template <int MODE, int STAGES>
+static int batch_occupancy_mode() {
+  const size_t smem = batch_smem_bytes_of<MODE, STAGES>();
+  auto kern = prop_batch_kernel<MODE, STAGES>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kThreads, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+#define SEPX_BATCH_CASES(X) \
+  X(kSrcProp, 3) X(kSrcProp, 4) X(kBornFwd, 3) X(kBornFwd, 4) X(kRtmAdj, 3) X(kRtmAdj, 4) X(kRtmAdj1, 3)
+
+cudaError_t launch_prop_multi(int mode, int stages, const MultiParams &mp, cudaStream_t st) {
+#define X(m, s) if (mode == m && stages == s) return launch_multi_mode<m, s>(mp, st);
+  SEPX_BATCH_CASES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+bool batch_supported(int mode, int stages) {
+#define X(m, s) if (mode == m && stages == s) return true;
+  SEPX_BATCH_CASES(X)
+#undef X
+  return false;
+}
+
+cudaError_t launch_prop_batch(int mode, int stages, const PropParams *params, const int4 *items,
+                              int nitems, const BatchStep &step, int grid, cudaStream_t st) {
+#define X(m, s) \
+  if (mode == m && stages == s) return launch_batch_mode<m, s>(params, items, nitems, step, grid, st);
+  SEPX_BATCH_CASES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+int prop_batch_occupancy(int mode, int stages) {
+#define X(m, s) if (mode == m && stages == s) return batch_occupancy_mode<m, s>();
+  SEPX_BATCH_CASES(X)
+#undef X
+  return 0;
 }
 
 size_t prop_smem_bytes(int mode) {

@@ -93,6 +93,31 @@ struct alignas(64) PropParams {
   void *snap;                 // storage
   float *snap_scale;          // per-block scale (power of two)
   int *err;                   // device error word
+  int inj_stride;             // batched launches: injection values per step (points)
+};
+
+// Parameter sets of up to kMaxMulti grids (shots) advanced by one launch:
+// CTA b is tile b of the concatenated tile lists (tile_base: prefix sums;
+// tiles of a grid numbered x fastest, then y, then z-chunk).  Held in the
+// kernel's parameter space (at most 32 KB), like the single-grid launch.
+constexpr int kMaxMulti = 18;
+struct MultiParams {
+  PropParams p[kMaxMulti];
+  int tile_base[kMaxMulti + 1];
+  int ntx[kMaxMulti];
+  int nty[kMaxMulti];
+  int nshot;
+};
+
+// Values of one time step shared by every parameter set of a batched launch:
+// inj_s advances by inj_row rows, sinc_row by sinc_ii rows of 8 taps.
+struct BatchStep {
+  int inj_row;
+  int trc_id;
+  int sinc_ii;
+  int do_scatter;
+  int do_image;
+  int parity;   // parameter set 2*shot + parity (the fields' ping-pong)
 };
 
 }  // namespace sepx

@@ -32,16 +32,21 @@ def same_bits(a, b):
 def _declared(header):
     txt = (ROOT / "include" / header).read_text()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    # C++ classes follow the extern "C" block in sepx_ops.h: only the C ABI counts
+    cut = txt.find('#ifdef __cplusplus\n}')
+    if cut > 0:
+        txt = txt[:cut]
     return sorted(set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt)) -
-                  {"if", "for", "while", "sizeof", "return"})
+                  {"if", "for", "while", "sizeof", "return", "int", "void"})
 
 
-@pytest.mark.parametrize("header", ["sepx.h", "sepx_host.h"])
+@pytest.mark.parametrize("header", ["sepx.h", "sepx_host.h", "sepx_ops.h", "sepx_batch.h",
+                                    "sepx_unet.h"])
 def test_library_exports_every_declared_symbol(header):
     from sep_code_gb300 import LIB_PATH
     lib = C.CDLL(str(LIB_PATH))
     names = _declared(header)
-    assert len(names) >= 8
+    assert len(names) >= 5
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
