@@ -31,38 +31,65 @@ constexpr int kTM = 128;   // GEMM rows per CTA (tensor-memory lanes)
 constexpr int kKC = 64;    // K per pipeline stage (8 K groups of 8)
 constexpr int kUThreads = 128;
 constexpr int kMaxN = 128;
-// spare shared memory after the two stages, so that operand reads through the
-// descriptors stay inside the CTA's allocation whatever the group strides
-constexpr int kSmemSlack = 64 * 1024;
 
 struct View {
   const __nv_bfloat16 *p;
   int cstride, coff;
 };
 
-__device__ __forceinline__ void tap_offset(int t, int ntap, int &dz, int &dy, int &dx) {
+// Voxel coordinates and the neighbour loads of the implicit GEMMs.  Volumes
+// hold fewer than 2^31 voxels (checked on the host), so voxel indices are
+// 32-bit; element offsets are formed from 64-bit row pointers.
+struct Coord {
+  int x, y, z;
+};
+
+__device__ __forceinline__ Coord coord_of(int v, int D, int H, int W) {
+  Coord c;
+  c.x = v % W;
+  const int r = v / W;
+  c.y = r % H;
+  c.z = (r / H) % D;
+  return c;
+}
+
+__device__ __forceinline__ void tap_delta(int t, int ntap, int &dz, int &dy, int &dx) {
   if (ntap == 1) {
     dz = dy = dx = 0;
   } else {
-    dz = t / 9 - 1;
-    dy = (t / 3) % 3 - 1;
-    dx = t % 3 - 1;
+    const int q = (t * 57) >> 9;   // t / 9 for 0 <= t < 27
+    dz = q - 1;
+    const int r = t - 9 * q;
+    const int q3 = (r * 11) >> 5;  // r / 3 for 0 <= r < 9
+    dy = q3 - 1;
+    dx = r - 3 * q3 - 1;
   }
 }
 
-// 16 bytes (8 channels) of voxel v shifted by tap t, or zeros outside the volume
-__device__ __forceinline__ uint4 gather8(const View &x, long long v, int D, int H, int W, int t,
-                                         int ntap, int c0) {
-  int dz, dy, dx;
-  tap_offset(t, ntap, dz, dy, dx);
-  const int xx = (int)(v % W);
-  const int yy = (int)((v / W) % H);
-  const int zz = (int)((v / ((long long)W * H)) % D);
-  const int x2 = xx + dx, y2 = yy + dy, z2 = zz + dz;
-  if (x2 < 0 || x2 >= W || y2 < 0 || y2 >= H || z2 < 0 || z2 >= D) return make_uint4(0, 0, 0, 0);
-  const long long v2 = v + (long long)dz * H * W + (long long)dy * W + dx;
-  return *reinterpret_cast<const uint4 *>(x.p + v2 * x.cstride + x.coff + c0);
+// 16 bytes (8 channels from channel c0) of the neighbour (dz, dy, dx) of the
+// voxel at (c) whose channel row starts at `row`, zeros outside the volume
+__device__ __forceinline__ uint4 load_nb(const __nv_bfloat16 *row, const Coord &c, int dz, int dy,
+                                         int dx, int D, int H, int W, int HWc, int Wc, int cs, int c0) {
+  const int x2 = c.x + dx, y2 = c.y + dy, z2 = c.z + dz;
+  if ((unsigned)x2 >= (unsigned)W || (unsigned)y2 >= (unsigned)H || (unsigned)z2 >= (unsigned)D)
+    return make_uint4(0, 0, 0, 0);
+  return *reinterpret_cast<const uint4 *>(row + (dz * HWc + dy * Wc + dx * cs + c0));
 }
+
+// 16-byte asynchronous copy global -> shared; src_bytes 0 fills zeros (src
+// must still be a valid address)
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+constexpr int kCS = 3;   // pipeline stages of the convolution kernels
 
 // ---------------------------------------------------------------------------
 // Forward (and data-gradient) convolution.
@@ -79,8 +106,8 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
   const int a_bytes = kTM * kKC * 2;      // 16 KB
   const int b_bytes = np * kKC * 2;       // <= 16 KB
   const int stage_bytes = a_bytes + b_bytes;
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + 2 * stage_bytes);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + kCS * stage_bytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + kCS);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long V = (long long)nb * D * H * W;
   const long long v0 = (long long)blockIdx.x * kTM;
@@ -91,8 +118,7 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    mbar_init(smem_u32(&bar[0]), 1);
-    mbar_init(smem_u32(&bar[1]), 1);
+    for (int i = 0; i < kCS; i++) mbar_init(smem_u32(&bar[i]), 1);
     mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -103,54 +129,84 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
   const int ngn = np / 8;
   bool ok = true;
   int last = -1;   // last chunk whose MMAs were committed
+  // this thread's output voxel (row `tid` of the tile) and its channel row
+  const int vr = (int)min(v0 + tid, V - 1);
+  const bool vin = v0 + tid < V;
+  const Coord cv = coord_of(vr, D, H, W);
+  const __nv_bfloat16 *xrow = x.p + (long long)vr * x.cstride + x.coff;
+  const int Wc = W * x.cstride, HWc = H * Wc;
+  int tap = 0, c0 = 0;   // K position of the next K group to fetch: tap and channel
 
-  for (int j = 0; j < kchunks; j++) {
-    const int s = j & 1;
-    if (j >= 2) {
-      // the MMAs of chunk j-2 have read this stage
-      if (!mbar_wait_bounded(smem_u32(&bar[s]), ((j - 2) >> 1) & 1, err, kErrMmaWait)) ok = false;
-    }
-    if (!__syncthreads_and(ok)) break;
-    unsigned char *A = sm + s * stage_bytes;
-    unsigned char *B = A + a_bytes;
-    // A: row = tid (one output voxel), 8 K groups of 8 channels of one tap
-    {
-      const int r = tid;
-      const long long v = v0 + r;
+  // chunk j -> stage j % kCS: the A row of this thread (8 K groups of 8
+  // channels of one tap, zeros outside the volume) and a share of the
+  // chunk's packed weights, as asynchronous copies (one commit group)
+  auto fetch = [&](int j) {
+    unsigned char *A = sm + (j % kCS) * stage_bytes;
+    unsigned char *Bm = A + a_bytes;
+    const int r = tid;
 #pragma unroll
-      for (int kg = 0; kg < kKC / 8; kg++) {
-        const int k0 = j * kKC + kg * 8;
-        const int t = k0 / cin, c0 = k0 - t * cin;
-        uint4 val = make_uint4(0, 0, 0, 0);
-        if (v < V && t < ntap) val = gather8(x, v, D, H, W, t, ntap, c0);
-        *reinterpret_cast<uint4 *>(A + (kg * (kTM / 8) + (r >> 3)) * 128 + (r & 7) * 16) = val;
+    for (int kg = 0; kg < kKC / 8; kg++) {
+      const __nv_bfloat16 *src = xrow;
+      int nbytes = 0;
+      if (vin && tap < ntap) {
+        int dz, dy, dx;
+        tap_delta(tap, ntap, dz, dy, dx);
+        const int x2 = cv.x + dx, y2 = cv.y + dy, z2 = cv.z + dz;
+        if ((unsigned)x2 < (unsigned)W && (unsigned)y2 < (unsigned)H && (unsigned)z2 < (unsigned)D) {
+          src = xrow + (dz * HWc + dy * Wc + dx * x.cstride + c0);
+          nbytes = 16;
+        }
+      }
+      cp_async16(A + (kg * (kTM / 8) + (r >> 3)) * 128 + (r & 7) * 16, src, nbytes);
+      c0 += 8;
+      if (c0 >= cin) {
+        c0 -= cin;
+        tap++;
       }
     }
-    // B: this chunk's packed weights, copied as they are
-    {
-      const uint4 *src = reinterpret_cast<const uint4 *>(wp + (size_t)j * np * kKC);
-      uint4 *dst = reinterpret_cast<uint4 *>(B);
-      for (int i = tid; i < b_bytes / 16; i += kUThreads) dst[i] = src[i];
-    }
+    const uint4 *wsrc = reinterpret_cast<const uint4 *>(wp + (size_t)j * np * kKC);
+    for (int i = tid; i < b_bytes / 16; i += kUThreads) cp_async16(Bm + 16 * i, wsrc + i, 16);
+    cp_async_commit();
+  };
+
+  for (int j = 0; j < kCS - 1; j++) {
+    if (j < kchunks) fetch(j);
+    else cp_async_commit();
+  }
+  for (int j = 0; j < kchunks; j++) {
+    cp_async_wait<kCS - 2>();   // this thread's copies of chunk j have landed
     tc::fence_proxy_async();
-    __syncthreads();
+    if (!__syncthreads_and(ok)) break;
     if (tid == 0) {
       tc::fence_after_sync();
-      const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+      unsigned char *A = sm + (j % kCS) * stage_bytes;
+      const uint32_t a0 = smem_u32(A), b0 = smem_u32(A + a_bytes);
 #pragma unroll
       for (int k16 = 0; k16 < kKC / 16; k16++) {
         const uint64_t ad = tc::smem_desc(a0 + k16 * 2 * (kTM / 8) * 128, (kTM / 8) * 128, 128);
         const uint64_t bd = tc::smem_desc(b0 + k16 * 2 * ngn * 128, ngn * 128, 128);
         tc::mma_bf16(tmem, ad, bd, idesc, (j > 0 || k16 > 0) ? 1u : 0u);
       }
-      tc::mma_commit(smem_u32(&bar[s]));
+      tc::mma_commit(smem_u32(&bar[j % kCS]));
     }
     last = j;
+    // refill: chunk j + kCS - 1 reuses the stage of chunk j - 1
+    const int jn = j + kCS - 1;
+    if (jn < kchunks) {
+      if (j >= 1 && !mbar_wait_bounded(smem_u32(&bar[(j - 1) % kCS]), ((j - 1) / kCS) & 1, err,
+                                       kErrMmaWait))
+        ok = false;
+      if (ok) fetch(jn);
+      else cp_async_commit();
+    } else {
+      cp_async_commit();
+    }
   }
+  cp_async_wait<0>();
   // all MMAs done (also on the error path, before the tensor memory is
   // freed): the last commit covers every earlier one
   if (last >= 0) {
-    if (!mbar_wait_bounded(smem_u32(&bar[last & 1]), (last >> 1) & 1, err, kErrMmaWait)) ok = false;
+    if (!mbar_wait_bounded(smem_u32(&bar[last % kCS]), (last / kCS) & 1, err, kErrMmaWait)) ok = false;
   }
   if (last != kchunks - 1) ok = false;
   ok = __syncthreads_and(ok);
@@ -209,8 +265,8 @@ __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
   const int a_bytes = kTM * kKC * 2;
   const int b_bytes = np * kKC * 2;
   const int stage_bytes = a_bytes + b_bytes;
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + 2 * stage_bytes);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + kCS * stage_bytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + kCS);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long V = (long long)nb * D * H * W;
   const int mtot = ntap * cin;
@@ -226,8 +282,7 @@ __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    mbar_init(smem_u32(&bar[0]), 1);
-    mbar_init(smem_u32(&bar[1]), 1);
+    for (int i = 0; i < kCS; i++) mbar_init(smem_u32(&bar[i]), 1);
     mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -238,54 +293,91 @@ __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
   const int ngn = np / 8;
   bool ok = true;
   int last = -1;
+  // this thread's A pieces: M group (tid % 16) -- one tap, 8 channels -- for
+  // the 8 consecutive voxels 8 * (tid / 16) .. +7 of every chunk
+  const int mg = tid % (kTM / 8), kv0 = (tid / (kTM / 8)) * 8;
+  const int m = m0 + mg * 8;
+  const bool m_in = m < mtot;
+  const int t_m = m_in ? m / cin : 0, c_m = m_in ? m - t_m * cin : 0;
+  int dzm, dym, dxm;
+  tap_delta(t_m, ntap, dzm, dym, dxm);
+  const int Wc = W * x.cstride, HWc = H * Wc;
 
-  for (int jj = 0; jj < nch; jj++) {
-    const int s = jj & 1;
-    if (jj >= 2) {
-      if (!mbar_wait_bounded(smem_u32(&bar[s]), ((jj - 2) >> 1) & 1, err, kErrMmaWait)) ok = false;
-    }
-    if (!__syncthreads_and(ok)) break;
-    unsigned char *A = sm + s * stage_bytes;
-    unsigned char *B = A + a_bytes;
+  // chunk jj (64 voxels) -> stage jj % kCS, asynchronous copies (one group)
+  auto fetch = [&](int jj) {
+    unsigned char *A = sm + (jj % kCS) * stage_bytes;
+    unsigned char *Bm = A + a_bytes;
     const long long vb = (jb + jj) * kKC;
-    // A: 16 M groups x 64 voxels of 16 bytes
-    for (int p = tid; p < (kTM / 8) * kKC; p += kUThreads) {
-      const int mg = p % (kTM / 8), kv = p / (kTM / 8);
-      const int m = m0 + mg * 8;
-      const long long v = vb + kv;
-      uint4 val = make_uint4(0, 0, 0, 0);
-      if (m < mtot && v < V) {
-        const int t = m / cin, c0 = m - t * cin;
-        val = gather8(x, v, D, H, W, t, ntap, c0);
+    int v = (int)(vb + kv0);
+    Coord c = coord_of(min(v, (int)V - 1), D, H, W);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int kv = kv0 + i;
+      const __nv_bfloat16 *row = x.p + (long long)min(v, (int)V - 1) * x.cstride + x.coff;
+      const __nv_bfloat16 *src = row;
+      int nbytes = 0;
+      if (m_in && v < V) {
+        const int x2 = c.x + dxm, y2 = c.y + dym, z2 = c.z + dzm;
+        if ((unsigned)x2 < (unsigned)W && (unsigned)y2 < (unsigned)H && (unsigned)z2 < (unsigned)D) {
+          src = row + (dzm * HWc + dym * Wc + dxm * x.cstride + c_m);
+          nbytes = 16;
+        }
       }
-      *reinterpret_cast<uint4 *>(A + ((kv >> 3) * (kTM / 8) + mg) * 128 + (kv & 7) * 16) = val;
+      cp_async16(A + ((kv >> 3) * (kTM / 8) + mg) * 128 + (kv & 7) * 16, src, nbytes);
+      v++;
+      if (++c.x == W) {
+        c.x = 0;
+        if (++c.y == H) {
+          c.y = 0;
+          if (++c.z == D) c.z = 0;
+        }
+      }
     }
-    // B: np/8 N groups x 64 voxels of dY
     for (int p = tid; p < ngn * kKC; p += kUThreads) {
       const int ng = p % ngn, kv = p / ngn;
-      const long long v = vb + kv;
-      uint4 val = make_uint4(0, 0, 0, 0);
-      if (v < V && ng * 8 < cout)
-        val = *reinterpret_cast<const uint4 *>(dy.p + v * dy.cstride + dy.coff + ng * 8);
-      *reinterpret_cast<uint4 *>(B + ((kv >> 3) * ngn + ng) * 128 + (kv & 7) * 16) = val;
+      const long long vv = vb + kv;
+      const bool in = vv < V && ng * 8 < cout;
+      const __nv_bfloat16 *src = dy.p + (in ? vv * dy.cstride + dy.coff + ng * 8 : dy.coff);
+      cp_async16(Bm + ((kv >> 3) * ngn + ng) * 128 + (kv & 7) * 16, src, in ? 16 : 0);
     }
+    cp_async_commit();
+  };
+
+  for (int jj = 0; jj < kCS - 1; jj++) {
+    if (jj < nch) fetch(jj);
+    else cp_async_commit();
+  }
+  for (int jj = 0; jj < nch; jj++) {
+    cp_async_wait<kCS - 2>();
     tc::fence_proxy_async();
-    __syncthreads();
+    if (!__syncthreads_and(ok)) break;
     if (tid == 0) {
       tc::fence_after_sync();
-      const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+      unsigned char *A = sm + (jj % kCS) * stage_bytes;
+      const uint32_t a0 = smem_u32(A), b0 = smem_u32(A + a_bytes);
 #pragma unroll
       for (int k16 = 0; k16 < kKC / 16; k16++) {
         const uint64_t ad = tc::smem_desc(a0 + k16 * 2 * (kTM / 8) * 128, (kTM / 8) * 128, 128);
         const uint64_t bd = tc::smem_desc(b0 + k16 * 2 * ngn * 128, ngn * 128, 128);
         tc::mma_bf16(tmem, ad, bd, idesc, (jj > 0 || k16 > 0) ? 1u : 0u);
       }
-      tc::mma_commit(smem_u32(&bar[s]));
+      tc::mma_commit(smem_u32(&bar[jj % kCS]));
     }
     last = jj;
+    const int jn = jj + kCS - 1;
+    if (jn < nch) {
+      if (jj >= 1 && !mbar_wait_bounded(smem_u32(&bar[(jj - 1) % kCS]), ((jj - 1) / kCS) & 1, err,
+                                        kErrMmaWait))
+        ok = false;
+      if (ok) fetch(jn);
+      else cp_async_commit();
+    } else {
+      cp_async_commit();
+    }
   }
+  cp_async_wait<0>();
   if (last >= 0) {
-    if (!mbar_wait_bounded(smem_u32(&bar[last & 1]), (last >> 1) & 1, err, kErrMmaWait)) ok = false;
+    if (!mbar_wait_bounded(smem_u32(&bar[last % kCS]), (last / kCS) & 1, err, kErrMmaWait)) ok = false;
   }
   if (last != nch - 1) ok = false;
   ok = __syncthreads_and(ok);
@@ -528,8 +620,13 @@ static int grid_for(long long n, int threads = 256) {
   return (int)(g < 1 ? 1 : (g > 8 * 152 * 4 ? 8 * 152 * 4 : g));
 }
 
+// kCS stages of A (16 KB) and B (np x 128 B), barriers, the tensor-memory
+// slot, alignment.  Resident CTAs per SM are bounded by this size, which also
+// keeps their tensor memory (np <= 32: 32 columns, <= 64: 64, else 128) within
+// the SM's 512 columns: 128 columns need np > 64, i.e. >= 78 KB, so at most 2
+// such CTAs; 64 columns need >= 57 KB (at most 3); 32 columns >= 54 KB (4).
 static size_t conv_smem(int np) {
-  return (size_t)2 * (kTM * kKC * 2 + np * kKC * 2) + 16 + 16 + 128 + kSmemSlack;
+  return (size_t)kCS * (kTM * kKC * 2 + np * kKC * 2) + 8 * kCS + 16 + 128;
 }
 
 }  // namespace sepx
@@ -591,6 +688,8 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
   const int np = np_of(cout);
   const int kch = (ntap * cin + kKC - 1) / kKC;
   const long long V = (long long)nb * D * H * W;
+  if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
+    return set_error("unet conv: volume too large (%lld voxels)", V);
   const size_t smem = conv_smem(np);
   static bool attr = false;
   if (!attr) {
@@ -617,6 +716,8 @@ int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D
   if (unet_err_ptr(&err)) return set_error("unet wgrad: cannot allocate the status word");
   const int np = np_of(cout);
   const long long V = (long long)nb * D * H * W;
+  if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
+    return set_error("unet wgrad: volume too large (%lld voxels)", V);
   const long long vchunks = (V + kKC - 1) / kKC;
   const int mt = (ntap * cin + kTM - 1) / kTM;
   // enough CTAs to fill the GPU about twice, at least 16 voxel chunks each
