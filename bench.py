@@ -301,6 +301,13 @@ def run_ours(args, ws, rank, dist):
             "avg_launch_ms": round(avg_launch * 1e3, 4),
             "traffic": traffic, "traffic_source": traffic_src,
             "loop_seconds": {k: round(v / args.steps, 4) for k, v in per_loop.items()},
+            # every loop's kernel against the same peak (the dominant one is above)
+            "per_kernel": {kernel_name[k]: {
+                "achieved_gbs": round(cells * bytes_per_cell[k] /
+                                      (per_loop[k] / (launches_per_loop[k] * args.steps)) / 1e9, 1),
+                "frac": round(cells * bytes_per_cell[k] /
+                              (per_loop[k] / (launches_per_loop[k] * args.steps)) / 1e9 / peak, 4),
+                "bytes_per_cell": bytes_per_cell[k]} for k in per_loop},
             "loop_gcells": {k: round(cells * fsteps[k] / (per_loop[k] / args.steps) / 1e9, 2)
                             for k in per_loop}}
 
@@ -384,10 +391,11 @@ def run_ours(args, ws, rank, dist):
 
 # ------------------------------------------------------------------ batched shots
 def run_batch(args):
-    """16 uneven-window shots on a 1024 x 1024 x 400 model: the Born forward
-    of every shot, shot after shot (the reference's shot loop) against one
-    persistent launch per step, with and without a captured CUDA graph, after
-    the autotuner picked the z-chunk and ring depth."""
+    """16 uneven-window shots on a 1024 x 1024 x 400 model: source_prop, Born
+    forward and RTM adjoint of every shot, shot after shot (the reference's
+    shot loops) against one launch per step for all shots, with and without a
+    captured CUDA graph, after the autotuner picked the Born forward's launch
+    style, z-chunk and ring depth."""
     import torch
     from sep_code_gb300 import batch as Bt
     nt = args.batch_nt
@@ -396,30 +404,38 @@ def run_batch(args):
     b = Bt.BatchRTM(surveys)
     t_setup = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(Bt.lib.sepx_get_stream())
-    updates = b.cell_updates()
-    out = {"metric": "Gcell-updates/s (batched Born forward, 16 shots)", "unit": "Gcell/s",
-           "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+    loops = ("source_prop", "forward", "adjoint")
+    updates = b.cell_updates(loops)
+    out = {"metric": "Gcell-updates/s (batched RTM, 16 shots: source_prop + Born forward + adjoint)",
+           "unit": "Gcell/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic",
            "config": {"workload": "batch_16_shots_1024x1024x400", "nt": nt,
                       "windows": [list(s.vel.shape[::-1]) for s in surveys],
                       "padded": ["x".join(map(str, st.n)) for st in b.setups],
-                      "cells_per_step": int(sum(b.cells))},
+                      "cells_per_field_step": int(sum(b.cells))},
            "setup_seconds": round(t_setup, 1)}
     z, st_, sty, ms = b.autotune(nsteps=8)
     out["autotune"] = {"zchunk": z, "stages": st_, "style": ["all-tiles", "persistent"][sty],
                        "ms_per_step": round(ms, 4)}
     res = {}
     for how in ("sequential", "persistent", "graph", "graph"):
-        b.zero_traces()
+        b.set_images()   # the previous adjoint wrote its image into the forward's input
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        evs[0].record(stream)
+        b.source_prop(how)
+        evs[1].record(stream)
+        b.zero_traces()
         b.forward(how)
-        e1.record(stream)
-        e1.synchronize()
-        sec = e0.elapsed_time(e1) / 1e3
+        evs[2].record(stream)
+        b.adjoint(how)
+        evs[3].record(stream)
+        evs[3].synchronize()
+        sec = evs[0].elapsed_time(evs[3]) / 1e3
         key = how if how not in res else how + "_replay"
-        res[key] = {"seconds": round(sec, 4), "gcells": round(updates / sec / 1e9, 2)}
+        res[key] = {"seconds": round(sec, 4), "gcells": round(updates / sec / 1e9, 2),
+                    "loop_seconds": {k: round(evs[i].elapsed_time(evs[i + 1]) / 1e3, 4)
+                                     for i, k in enumerate(loops)}}
     b.close()
     out["runs"] = res
     out["value"] = res["graph_replay"]["gcells"]

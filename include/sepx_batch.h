@@ -31,6 +31,11 @@ int sepx_batch_end(void);
  * CUDA graph once and replayed (re-captured when nt, jt or the tuning
  * change).  Every shot must use the same jt and nt. */
 int sepx_batch_rtm_forward(int jt, int npts_src, int nt, int how);
+/* the same for source_prop (nt + 1 steps; the two last fields kept per shot)
+ * and for rtm_adjoint on those fields (sepx_rtm_adjoint_resident semantics
+ * with use_source_last = 1: image per shot via sepx_get_image) */
+int sepx_batch_source_prop(int jt, int npts, int nt, int how);
+int sepx_batch_rtm_adjoint(int jt, int npts, int nt, int how);
 /* time nsteps batched steps for every style x z-chunk x ring-depth candidate,
  * keep the fastest (clears every shot's receiver traces) */
 int sepx_batch_autotune(int jt, int npts_src, int nsteps, int *zchunk, int *stages, int *style,

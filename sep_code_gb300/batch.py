@@ -22,12 +22,15 @@ from ._lib import SepxError, lib
 lib.sepx_batch_begin.argtypes = [C.c_int]
 lib.sepx_batch_select.argtypes = [C.c_int]
 lib.sepx_batch_rtm_forward.argtypes = [C.c_int] * 4
+lib.sepx_batch_source_prop.argtypes = [C.c_int] * 4
+lib.sepx_batch_rtm_adjoint.argtypes = [C.c_int] * 4
 lib.sepx_batch_autotune.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(C.c_int), C.POINTER(C.c_float)]
 lib.sepx_batch_set_tuning.argtypes = [C.c_int, C.c_int, C.c_int]
 lib.sepx_batch_get_tuning.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
 for _n in ("sepx_batch_begin", "sepx_batch_select", "sepx_batch_size", "sepx_batch_end",
-           "sepx_batch_rtm_forward", "sepx_batch_autotune", "sepx_batch_set_tuning",
+           "sepx_batch_rtm_forward", "sepx_batch_source_prop", "sepx_batch_rtm_adjoint",
+           "sepx_batch_autotune", "sepx_batch_set_tuning",
            "sepx_batch_get_tuning"):
     getattr(lib, _n).restype = C.c_int
 
@@ -117,8 +120,57 @@ class BatchRTM:
             gf.zero_traces()
         lib.sepx_batch_select(-1)
 
+    def _each(self, fn):
+        try:
+            for i in range(len(self.setups)):
+                _chk(lib.sepx_batch_select(i))
+                fn(i)
+        finally:
+            lib.sepx_batch_select(-1)
+
+    def source_prop(self, how: str = "graph"):
+        """create_source_fields for every shot: source traces of nt+9 samples"""
+        def up(i):
+            s, st = self.surveys[i], self.setups[i]
+            wd = gf.wavelet_deriv(s.wavelet, s.dtw)
+            sx, sy, sz = s.shots[0]
+            locs, vals = gf.source_func(wd, sx, sy, sz, st.n[0], st.n[1], st.o, st.d, s.data_nt + 9)
+            gf.transfer_source_func(locs, vals)
+        self._each(up)
+        _chk(lib.sepx_batch_source_prop(self.setups[0].jts, 9, self.nt, HOW[how]))
+
+    def _forward_sources(self):
+        self._each(lambda i: gf.transfer_source_func(self.setups[i].src_locs, self.setups[i].src_vals))
+
     def forward(self, how: str = "graph"):
+        """Born forward of every shot (source traces of nt+8 samples)"""
+        self._forward_sources()
         _chk(lib.sepx_batch_rtm_forward(self.jt, 9, self.nt, HOW[how]))
+
+    def adjoint(self, how: str = "graph"):
+        """RTM adjoint of every shot from its receiver traces and last source_prop"""
+        self._forward_sources()
+        _chk(lib.sepx_batch_rtm_adjoint(self.jt, 9, self.nt, HOW[how]))
+
+    def set_images(self):
+        """upload every shot's reflectivity image (the Born forward's input;
+        the adjoint writes its RTM image into the same device buffer)"""
+        self._each(lambda i: gf.set_image(self.setups[i].img_lap))
+
+    def image(self, i):
+        st = self.setups[i]
+        _chk(lib.sepx_batch_select(i))
+        try:
+            return gf.get_image((st.n[2], st.n[1], st.n[0]))
+        finally:
+            lib.sepx_batch_select(-1)
+
+    def rtm(self, how: str = "graph"):
+        """the bench step of every shot: source_prop, Born forward, adjoint"""
+        self.source_prop(how)
+        self.zero_traces()
+        self.forward(how)
+        self.adjoint(how)
 
     def traces(self, i):
         st = self.setups[i]
@@ -138,6 +190,7 @@ class BatchRTM:
     def set_tuning(self, zchunk: int, stages: int, style: int = 0):
         _chk(lib.sepx_batch_set_tuning(zchunk, stages, style))
 
-    def cell_updates(self):
-        """updated cells x fields x steps of one Born forward of the batch"""
-        return 2 * self.nt * sum(self.cells)
+    def cell_updates(self, loops=("forward",)):
+        """updated cells x fields x steps of the given loops over the batch"""
+        per = {"source_prop": self.nt + 1, "forward": 2 * self.nt, "adjoint": 2 * self.nt - 1}
+        return sum(per[k] for k in loops) * sum(self.cells)

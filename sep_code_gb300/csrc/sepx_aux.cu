@@ -63,6 +63,20 @@ cudaError_t launch_inj_values(const float *src, int ntrace, int npts, const floa
   return cudaGetLastError();
 }
 
+// One thread per grid: its points in order (several points may share a cell).
+__global__ void point_add_multi_kernel(const PointAddSets sets) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= sets.n) return;
+  const PointAddSet &s = sets.s[g];
+  for (int i = 0; i < s.npts; i++) s.p[s.off[i]] = __fadd_rn(s.p[s.off[i]], s.inj[i]);
+}
+
+cudaError_t launch_point_add_multi(const PointAddSets &sets, cudaStream_t st) {
+  if (sets.n <= 0) return cudaSuccess;
+  point_add_multi_kernel<<<1, 32, 0, st>>>(sets);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_point_add(float *p, const long long *off, const float *inj, int npts,
                              cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;

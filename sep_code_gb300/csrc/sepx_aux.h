@@ -19,6 +19,18 @@ cudaError_t launch_inj_values(const float *src, int ntrace, int npts, const floa
                               int jt, int nsteps, int j0, float dir, float *out, cudaStream_t st);
 cudaError_t launch_point_add(float *p, const long long *off, const float *inj, int npts,
                              cudaStream_t st);
+// point adds of up to kMaxMulti grids in one launch
+struct PointAddSet {
+  float *p;
+  const long long *off;
+  const float *inj;
+  int npts;
+};
+struct PointAddSets {
+  PointAddSet s[kMaxMulti];
+  int n;
+};
+cudaError_t launch_point_add_multi(const PointAddSets &sets, cudaStream_t st);
 cudaError_t launch_transpose(const float *in, long long lda, float *out, long long ldb, int rows,
                              int cols, cudaStream_t st);
 

@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB)
 
 // Many shots (or any set of grids) in one persistent launch: CTA b runs the
 // tiles b, b + gridDim.x, ... of the item list.  Item = (shot, tile x, tile
-// y, z-chunk), parameter set 2*shot + the step's parity; the parameter set's scalars are copied into shared
+// y, z-chunk), parameter set pstride*shot + the step's set; the parameter set's scalars are copied into shared
 // memory and the step's values patched in (injection row, trace sample,
 // sinc row, scattering / imaging switches), its tensor maps read from global
 // memory.
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(kThreads, batch_minb<MODE>())
       reinterpret_cast<unsigned char *>(smem) + ((smem_carve_bytes<MODE, STAGES>() + 63) & ~size_t(63)));
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int4 item = items[it];
-    const PropParams *Pg = params + 2 * item.x + step.parity;
+    const PropParams *Pg = params + step.pstride * item.x + step.pset;
     const uint4 *src = reinterpret_cast<const uint4 *>(Pg);
     uint4 *dst = reinterpret_cast<uint4 *>(Ps);
     for (int i = threadIdx.x; i < (int)(sizeof(PropParams) / 16); i += kThreads) dst[i] = src[i];

@@ -117,7 +117,8 @@ struct BatchStep {
   int sinc_ii;
   int do_scatter;
   int do_image;
-  int parity;   // parameter set 2*shot + parity (the fields' ping-pong)
+  int pset;      // parameter set pstride*shot + pset (the fields' ping-pong)
+  int pstride;
 };
 
 }  // namespace sepx

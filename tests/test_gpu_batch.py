@@ -73,3 +73,26 @@ def test_batch_shot_equals_single_context():
         st = M.prepare_shot(s)
         single = GpuShot(s, st).rtm_forward(st.img_lap)
         assert np.array_equal(single, t)
+
+
+@pytest.mark.parametrize("style", [0, 1])
+def test_batched_full_rtm_equals_sequential(style):
+    """source_prop + Born forward + RTM adjoint of every shot: batched (one
+    launch per step, plain and captured) against the shot loop, images and
+    traces bit for bit"""
+    b = Bt.BatchRTM(_surveys())
+    try:
+        b.set_tuning(0, 3, style)
+        b.set_images()
+        b.rtm("sequential")
+        want_img = [b.image(i) for i in range(len(b.setups))]
+        want_trc = [b.traces(i) for i in range(len(b.setups))]
+        assert all(np.abs(im).max() > 0 for im in want_img)
+        for how in ("persistent", "graph", "graph"):
+            b.set_images()   # the adjoint overwrote each shot's image buffer
+            b.rtm(how)
+            for i in range(len(b.setups)):
+                assert np.array_equal(b.traces(i), want_trc[i]), (how, i)
+                assert np.array_equal(b.image(i), want_img[i]), (how, i)
+    finally:
+        b.close()
