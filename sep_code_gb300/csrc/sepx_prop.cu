@@ -33,6 +33,7 @@
 
 #include "sepx_device.cuh"
 #include "sepx_prop.h"
+#include "sepx_tc.cuh"
 
 // Resident CTAs per SM the register budget targets, and ring depths, of the
 // two heaviest modes (compile-time tuning knobs; the defaults measured best
@@ -42,6 +43,11 @@
 #endif
 #ifndef SEPX_ADJ_MINB
 #define SEPX_ADJ_MINB 3
+#endif
+// 1: the z-queues of the Born forward live in tensor memory (tcgen05.ld/st)
+// instead of registers
+#ifndef SEPX_TMEMQ
+#define SEPX_TMEMQ 0
 #endif
 #ifndef SEPX_FWD_STAGES
 #define SEPX_FWD_STAGES 3
@@ -91,6 +97,12 @@ struct Mode {
             (VEL_HALO ? kHaloFloats : kCenterFloats) + NF * kCenterFloats +
             (HAS_AUX ? kCenterFloats : 0));
   static constexpr uint32_t BYTES_IMG = BYTES_NOIMG + (HAS_IMG ? 4u * kCenterFloats : 0u);
+  // TQ: the z-queues of the current fields live in tensor memory: per field
+  // 16 slots of 4 columns (planes w and w+8 of a ring of 8, so the 8 planes
+  // z-4 .. z+3 of every step are 32 consecutive columns); the z+4 feed is
+  // read from shared memory and written to both copies of its slot
+  static constexpr bool TQ = SEPX_TMEMQ && MODE == kBornFwd;
+  static constexpr uint32_t TQ_COLS = NF == 2 ? 128u : 64u;
   // resident blocks per SM the register budget is sized for
   static constexpr int MINB = (MODE == kSrcProp)  ? 4
                               : (MODE == kBornFwd) ? SEPX_FWD_MINB
@@ -245,7 +257,7 @@ __host__ __device__ constexpr size_t smem_carve_bytes() {
 // flight and its barriers invalidated, so that the next tile may start.
 template <int MODE, int STAGES>
 __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &T, int bx, int by,
-                                         int bz, float *smem) {
+                                         int bz, float *smem, uint32_t tq_base) {
   using M = Mode<MODE>;
   constexpr int NF = M::NF;
   unsigned long long *bar_full = reinterpret_cast<unsigned long long *>(smem + STAGES * M::STAGE);
@@ -333,16 +345,27 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
     };
     int src_next = src_slot(za), rec_next = rec_slot(za);
     float4 q[NF][9];
+    // M::TQ: this warp's lanes of the z-queues in tensor memory (allocated by
+    // the kernel once, for every tile it runs)
+    const uint32_t tq = tq_base + ((uint32_t)(warp * 32) << 16);
     // warm-up: planes za-4 .. za+3 of the current field(s) along z
-    if (active) {
+    if (active || M::TQ) {
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const long long off = rowoff + g.plane * (za - 4 + j);
 #pragma unroll
         for (int f = 0; f < NF; f++) {
-          float4 p = ldg4(P.cur[f] + off);
-          if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, ldg4(P.vel + off));
-          q[f][j] = p;
+          float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (active) {
+            p = ldg4(P.cur[f] + off);
+            if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, ldg4(P.vel + off));
+          }
+          if (M::TQ) {
+            tc::tmem_st4(tq + f * 64 + 4 * j, p);
+            tc::tmem_st4(tq + f * 64 + 4 * (j + 8), p);
+          } else {
+            q[f][j] = p;
+          }
         }
       }
     }
@@ -350,8 +373,17 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
     const int coff = row * kTX + 4 * xq;             // centre tile
     for (int i = 0; i < niter; i++) {
       const int s = i % STAGES;
-      if (!mbar_wait_bounded(smem_u32(&bar_full[s]), (i / STAGES) & 1, P.err, kErrFullWait))
+      const bool ok = mbar_wait_bounded(smem_u32(&bar_full[s]), (i / STAGES) & 1, P.err, kErrFullWait);
+      if (M::TQ) {
+        // tensor-memory operations are warp-wide: leave the loop together
+        if (!__all_sync(0xffffffffu, ok)) break;
+        tc::tmem_wait_st();   // the previous plane's feed is in place
+#pragma unroll
+        for (int f = 0; f < NF; f++) tc::tmem_ld32_q8(tq + f * 64 + 4 * (i & 7), q[f]);
+        q[0][8] = q[NF - 1][8] = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else if (!ok) {
         break;
+      }
       const float *st = smem + s * M::STAGE;
       const int z = za + i;
       const int src_sl = src_next, rec_sl = rec_next;
@@ -610,12 +642,23 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
           stcs4(P.out[f] + cell, make_float4(o[0], o[1], o[2], o[3]));
         }
         // advance the z-queues
+        if (!M::TQ) {
 #pragma unroll
-        for (int f = 0; f < NF; f++)
+          for (int f = 0; f < NF; f++)
 #pragma unroll
-          for (int j = 0; j < 8; j++) q[f][j] = q[f][j + 1];
+            for (int j = 0; j < 8; j++) q[f][j] = q[f][j + 1];
+        }
+      }
+      if (M::TQ) {
+        // the z+4 plane replaces z-4 (slot i & 7 and its copy)
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          tc::tmem_st4(tq + f * 64 + 4 * (i & 7), q[f][8]);
+          tc::tmem_st4(tq + f * 64 + 4 * ((i & 7) + 8), q[f][8]);
+        }
       }
     }
+    if (M::TQ) tc::tmem_wait_st();   // each warp owns its lanes: no barrier needed
   }
 
   // Drain: never leave the CTA with bulk copies still writing its shared memory.
@@ -636,11 +679,50 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
   }
 }
 
+// Tensor memory of the z-queues (M::TQ): warp 0 allocates it once per CTA
+// before any tile, and frees it after the last (a CTA may allocate only until
+// it relinquishes its permit).  Shared memory per CTA bounds the resident CTAs
+// (3, or 2 for the persistent kernel) so that 128 columns each fit the SM's 512.
+template <int MODE>
+__device__ __forceinline__ uint32_t tq_alloc(float *smem_slot) {
+  using M = Mode<MODE>;
+  if (!M::TQ) return 0;
+  uint32_t *slot = reinterpret_cast<uint32_t *>(smem_slot);
+  if (threadIdx.x < 32) {
+    tc::tmem_alloc(smem_u32(slot), M::TQ_COLS);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  return *slot;
+}
+template <int MODE>
+__device__ __forceinline__ void tq_free(uint32_t base) {
+  using M = Mode<MODE>;
+  if (!M::TQ) return;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (threadIdx.x < 32) tc::tmem_dealloc(base, M::TQ_COLS);
+}
+
+// the 4-float block-max slot of the carve holds the tensor-memory address
+// (the TQ modes do not use the block max)
+template <int MODE, int STAGES>
+__device__ __forceinline__ float *tq_slot(float *smem) {
+  return reinterpret_cast<float *>(reinterpret_cast<unsigned long long *>(
+                                       smem + STAGES * Mode<MODE>::STAGE) + 2 * STAGES);
+}
+
 template <int MODE, int STAGES>
 __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB)
     prop_step_kernel(const __grid_constant__ PropParams P) {
   extern __shared__ unsigned char smem_raw[];
-  run_tile<MODE, STAGES>(P, P, blockIdx.x, blockIdx.y, blockIdx.z, smem_base<MODE, STAGES>(smem_raw));
+  float *smem = smem_base<MODE, STAGES>(smem_raw);
+  const uint32_t tq = tq_alloc<MODE>(tq_slot<MODE, STAGES>(smem));
+  run_tile<MODE, STAGES>(P, P, blockIdx.x, blockIdx.y, blockIdx.z, smem, tq);
+  tq_free<MODE>(tq);
 }
 
 // Many shots (or any set of grids) in one persistent launch: CTA b runs the
@@ -665,6 +747,7 @@ __global__ void __launch_bounds__(kThreads, batch_minb<MODE>())
   float *smem = smem_base<MODE, STAGES>(smem_raw);
   PropParams *Ps = reinterpret_cast<PropParams *>(
       reinterpret_cast<unsigned char *>(smem) + ((smem_carve_bytes<MODE, STAGES>() + 63) & ~size_t(63)));
+  const uint32_t tq = tq_alloc<MODE>(tq_slot<MODE, STAGES>(smem));
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int4 item = items[it];
     const PropParams *Pg = params + step.pstride * item.x + step.pset;
@@ -680,9 +763,10 @@ __global__ void __launch_bounds__(kThreads, batch_minb<MODE>())
       Ps->do_image = step.do_image;
     }
     __syncthreads();
-    run_tile<MODE, STAGES>(*Ps, *Pg, item.y, item.z, item.w, smem);
+    run_tile<MODE, STAGES>(*Ps, *Pg, item.y, item.z, item.w, smem, tq);
     __syncthreads();
   }
+  tq_free<MODE>(tq);
 }
 
 // Up to kMaxMulti grids in one launch, parameters in parameter space.
@@ -696,7 +780,10 @@ __global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB)
   const int local = b - mp.tile_base[s];
   const int ntx = mp.ntx[s], nty = mp.nty[s];
   const int bx = local % ntx, by = (local / ntx) % nty, bz = local / (ntx * nty);
-  run_tile<MODE, STAGES>(mp.p[s], mp.p[s], bx, by, bz, smem_base<MODE, STAGES>(smem_raw));
+  float *smem = smem_base<MODE, STAGES>(smem_raw);
+  const uint32_t tq = tq_alloc<MODE>(tq_slot<MODE, STAGES>(smem));
+  run_tile<MODE, STAGES>(mp.p[s], mp.p[s], bx, by, bz, smem, tq);
+  tq_free<MODE>(tq);
 }
 
 template <int MODE, int STAGES>

@@ -100,5 +100,45 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Eight 32-lane x 4-column loads (columns col + 4j .. col + 4j + 3, j = 0..7,
+// each naturally aligned) into q[0..7]; thread t reads lane (32 * (warp % 4)
+// + t).  Loads and the wait in one block: the registers are valid after it.
+__device__ __forceinline__ void tmem_ld32_q8(uint32_t taddr, float4 (&q)[9]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%32];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4, %5, %6, %7}, [%33];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8, %9, %10, %11}, [%34];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%12, %13, %14, %15}, [%35];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16, %17, %18, %19}, [%36];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20, %21, %22, %23}, [%37];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%24, %25, %26, %27}, [%38];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%28, %29, %30, %31}, [%39];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr), "r"(taddr + 4), "r"(taddr + 8), "r"(taddr + 12), "r"(taddr + 16),
+        "r"(taddr + 20), "r"(taddr + 24), "r"(taddr + 28)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 8; j++)
+    q[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                       __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+}
+
+// 32 lanes x 4 columns from the calling thread's float4
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, float4 v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr),
+               "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
+               "r"(__float_as_uint(v.w))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 }  // namespace tc
 }  // namespace sepx

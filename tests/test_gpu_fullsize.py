@@ -1,0 +1,66 @@
+"""Size-independent properties of the CUDA path at the full single-shot RTM
+workload (512 x 512 x 400 model, padded 560 x 560 x 496, 4000 steps, 262,144
+receivers), where the CPU oracle would need hours: the Born forward is linear
+in the image and the RTM adjoint linear in the data, so doubling the input
+doubles the output.  Doubling commutes with every rounding except in the
+subnormal range: ahead of each wavefront the fields decay through subnormal
+values, whose rounding is absolute rather than relative, and those
+differences travel with the front.  The FP32 oracle shows the same (relative
+L2 ~1e-6 at 48^3 x 400 steps; tests/test_pins_cpu.py pins it at 32^3), so the bar here is the
+parity bar, relative L2 <= 1e-5, not bit equality."""
+import numpy as np
+import pytest
+
+from sep_code_gb300 import gpu_funcs as gf
+from sep_code_gb300._lib import lib
+from tests.harness import rel_l2
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+
+def _chk(rc):
+    if rc:
+        raise gf.SepxError(lib.sepx_last_error().decode())
+
+
+def test_full_size_linearity():
+    from sep_code_gb300 import model as M
+    s = M.config2_survey()
+    st = M.prepare_shot(s)
+    n1, n2, n3 = st.n
+    nrec = st.rnx * st.rny
+    wd = gf.wavelet_deriv(s.wavelet, s.dtw)
+    sx, sy, sz = s.shots[0]
+    locs9, vals9 = gf.source_func(wd, sx, sy, sz, n1, n2, st.o, st.d, s.data_nt + 9)
+    gf.setup_cuda(1)
+    gf.create_gpu_space(st.d[0], st.d[1], st.d[2], s.bc_a, s.bc_b, s.bc_b, n1, n2, n3)
+    gf.transfer_sinc_table_s(st.sinc_s)
+    gf.transfer_sinc_table_d(st.sinc_d)
+    gf.transfer_vel_func1(st.vel2dt2)
+    gf.transfer_receiver_func(st.rnx, st.rny, st.rec_locs, np.zeros((nrec, st.nt_big), np.float32))
+    gf.transfer_source_func(locs9, vals9)
+    _chk(lib.sepx_source_prop_resident(st.jts, 9, st.nt))
+    gf.transfer_source_func(st.src_locs, st.src_vals)
+
+    def forward(img):
+        gf.set_image(img)
+        gf.zero_traces()
+        _chk(lib.sepx_rtm_forward_resident(st.jtd, 9, st.nt))
+        return gf.get_traces(nrec, st.nt_big)
+
+    img = np.ascontiguousarray(st.img_lap, np.float32)
+    d1 = forward(img)
+    d2 = forward(2 * img)
+    assert np.abs(d1).max() > 0
+    assert rel_l2(d2, 2 * d1) <= 1e-5
+
+    def adjoint(d):
+        gf.set_traces(d)
+        _chk(lib.sepx_rtm_adjoint_resident(st.jtd, 9, st.nt, 1))
+        return gf.get_image((n3, n2, n1))
+
+    i1 = adjoint(d1)
+    i2 = adjoint(2 * d1)
+    assert np.abs(i1).max() > 0
+    assert rel_l2(i2, 2 * i1) <= 1e-5
+    assert gf.device_error() == 0
