@@ -148,6 +148,24 @@ int sepx_op_padded_to_image(float *model, int m1, int m2, int m3, int f1, int f2
 int sepx_op_traces_to_data(float *data, int nt, float dt);
 int sepx_op_data_to_traces(const float *data, int nt, float dt);
 
+/* Image and data vectors kept in HBM, on the context stream (the reference
+ * keeps them in out-of-core SEP files and loops over them on the host):
+ * image_add_window:     image_rtm_3d::add_image (Born/image_rtm_3d.cpp:24-49):
+ *   img[n3][n2][n1] cell j + f += sub[s3][s2][s1] cell j, where inside img;
+ * image_extract_window: image_rtm_3d::extract_sub (:52-90): sub cell j =
+ *   img * mute at j + f (mute NULL: 1), 0 outside img;
+ * tmute:                tmute::forward / adjoint (Born/tmute.cpp:4-76) on
+ *   [nrep][n2][n1] traces: data (+)= model (adj: model (+)= data) from sample
+ *   (int)((t0 + (o2 + d2 i2) / vmute - o1) / d1) of trace i2 on (a start
+ *   before the first sample is taken as 0); add = 0 zeroes the output first.
+ * All buffers are device pointers. */
+int sepx_image_add_window(float *img, int n1, int n2, int n3, int f1, int f2, int f3,
+                          const float *sub, int s1, int s2, int s3);
+int sepx_image_extract_window(const float *img, const float *mute, int n1, int n2, int n3, int f1,
+                              int f2, int f3, float *sub, int s1, int s2, int s3);
+int sepx_tmute(int adj, int add, float t0, float vmute, int n1, float o1, float d1, int n2, float o2,
+               float d2, long long nrep, float *model, float *data);
+
 /* Device float vectors and BLAS-1 on the context stream (hypercube_float,
  * Born/hypercube_float.cpp:123-223; scale factors applied in double). */
 int sepx_vec_alloc(float **p, long long n);

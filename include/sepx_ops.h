@@ -66,6 +66,32 @@ int sepx_lsrtm(sepx_op_handle op, const float *data, int niter, float *model, do
                double *seconds, sepx_direction_fn dir, void *dir_ctx, double fallback_ratio,
                int *fallback_iter);
 
+/* When the search direction is preconditioned (the learned direction of the
+ * least-squares RTM; no counterpart in the reference, whose solver is plain
+ * Born/lin_solver.cpp:115-143):
+ *  SEPX_DIR_FALLBACK  as sepx_lsrtm: preconditioned until one step lowers
+ *                     rr.rr by less than fallback_ratio allows, then plain g;
+ *  SEPX_DIR_ADAPTIVE  preconditioned while its steps lower rr.rr by at least
+ *                     as large a fraction as the latest plain step did (before
+ *                     the first plain step: the fallback_ratio rule); after a
+ *                     switch to plain g the preconditioned direction is tried
+ *                     again every probe_every plain iterations. */
+enum { SEPX_DIR_FALLBACK = 0, SEPX_DIR_ADAPTIVE = 1 };
+typedef struct {
+  sepx_direction_fn dir;   /* NULL: plain simple_solver + cgstep */
+  void *dir_ctx;
+  int policy;              /* SEPX_DIR_FALLBACK | SEPX_DIR_ADAPTIVE */
+  double fallback_ratio;
+  int probe_every;         /* SEPX_DIR_ADAPTIVE, >= 1 */
+  double target;           /* > 0: stop once sqrt(rr.rr / rr0.rr0) <= target */
+} sepx_lsrtm_opts;
+/* sepx_lsrtm with a direction policy and a stopping residual: runs at most
+ * niter iterations; resid / seconds / used_dir (1 where the preconditioned
+ * direction was used; each may be NULL) are written for the iterations run,
+ * -1 after them; *iters_done (may be NULL) is the number run. */
+int sepx_lsrtm_ex(sepx_op_handle op, const float *data, int niter, const sepx_lsrtm_opts *opts,
+                  float *model, double *resid, double *seconds, int *used_dir, int *iters_done);
+
 #ifdef __cplusplus
 }
 
@@ -222,8 +248,12 @@ class lin_solver {
   sepx_direction_fn dir = nullptr;
   void *dir_ctx = nullptr;
   double fallback_ratio = 0.0;   // > 0: switch to plain g once a step gains less
-  int fallback_iter = -1;
+  int fallback_iter = -1;        // first iteration after which plain g was chosen
+  int dir_policy = SEPX_DIR_FALLBACK;
+  int probe_every = 8;
+  double target = 0.0;           // > 0: stop at this residual relative to the initial one
   std::vector<double> resid, seconds;
+  std::vector<int> used_dir;
   my_vector *g = nullptr, *m = nullptr, *gg = nullptr, *rr = nullptr;
   my_operator *oper = nullptr;
   step *st = nullptr;
@@ -272,6 +302,44 @@ class rtm_zero_op : public my_operator {
   struct shot_setup;
   struct impl;
   impl *d = nullptr;
+};
+
+// Time mute (Born/tmute.h, Born/tmute.cpp:4-76): the samples of trace i2 from
+// t_0 + x / vmute on (x = o2 + d2 i2, the axis-2 coordinate) pass, the earlier
+// ones are removed.  Model and data: hypercube_float of the same shape, axes
+// (t, x, ...).  forward of the reference moves its file cursor a whole cube per
+// axis-3 index; here both directions apply the mask to every cube.
+class tmute : public my_operator {
+ public:
+  tmute(float t, float v, my_vector *mod, my_vector *dat);
+  bool forward(bool add, my_vector *model, my_vector *data, int iter = 1) override;
+  bool adjoint(bool add, my_vector *model, my_vector *data, int iter = 1) override;
+  float t_0, vmute;
+};
+
+// The image of a migration on its grid (Born/image_rtm_3d.h): sub-images
+// (e.g. one shot's window) are added at the offset their origins give, and
+// windows are read back through the mute.  mute == nullptr acts as 1.
+class image_rtm_3d {
+ public:
+  explicit image_rtm_3d(const std::vector<axis> &axes);
+  ~image_rtm_3d();
+  image_rtm_3d(const image_rtm_3d &) = delete;
+  void set_mute(const hypercube_float &m);          // copies m (same shape)
+  void add_image(const hypercube_float *img);       // image_rtm_3d.cpp:24-49
+  hypercube_float *extract_sub(axis a1, axis a2, axis a3) const;   // :52-90
+  void write_volume();                              // image *= mute (:92-104)
+  axis get_axis(int i) const { return image->get_axis(i); }
+  hypercube_float *image = nullptr, *mute = nullptr;
+};
+
+// Multi-shot data (Born/data_rtm_3d.h): axes (t, x, y, shot); add_data
+// accumulates one shot's traces (data_rtm_3d.cpp:37-51).
+class data_rtm_3d : public hypercube_float {
+ public:
+  explicit data_rtm_3d(const std::vector<axis> &axes);
+  void add_data(int ishot, const hypercube_float *dat);
+  int nshots() const;   // product of the axes after the third
 };
 
 #endif /* __cplusplus */

@@ -301,6 +301,60 @@ class RefHost:
         self.lib.ref_map_data(int(fwd), int(add), ntb, nt, n2, n3, m, d)
         return m, d
 
+    # ---- image / data vectors (Born/image_rtm_3d.cpp, data_rtm_3d.cpp, tmute.cpp) ----
+    def _dataimg_sigs(self):
+        L = self.lib
+        if getattr(self, "_di", False):
+            return L
+        I3 = np.ctypeslib.ndpointer(np.int32, shape=(3,), flags="C_CONTIGUOUS")
+        F3 = np.ctypeslib.ndpointer(np.float32, shape=(3,), flags="C_CONTIGUOUS")
+        L.ref_image_add.argtypes = [I3, F3, F3, F32P, I3, F3, F3, F32P]
+        L.ref_image_extract.argtypes = [I3, F3, F3, F32P, F32P, I3, F3, F3, F32P, F32P]
+        L.ref_add_data.argtypes = [C.c_int] * 4 + [F32P, C.c_int, F32P]
+        L.ref_tmute.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float,
+                                C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, F32P, F32P]
+        self._di = True
+        return L
+
+    @staticmethod
+    def _grid(shape, o, d):
+        return (np.array(shape[::-1], np.int32), np.array(o, np.float32), np.array(d, np.float32))
+
+    def image_add(self, img, o, d, sub, so, sd):
+        """image_rtm_3d::add_image; img/sub [n3][n2][n1], o/d per axis (1, 2, 3)"""
+        L = self._dataimg_sigs()
+        out = np.ascontiguousarray(img, np.float32).copy()
+        L.ref_image_add(*self._grid(out.shape, o, d), out, *self._grid(sub.shape, so, sd),
+                        np.ascontiguousarray(sub, np.float32))
+        return out
+
+    def image_extract(self, img, mute, o, d, sub_shape, so, sd):
+        """image_rtm_3d::extract_sub and write_volume: (sub, img * mute)"""
+        L = self._dataimg_sigs()
+        img = np.ascontiguousarray(img, np.float32)
+        sub = np.zeros(sub_shape, np.float32)
+        muted = np.zeros_like(img)
+        L.ref_image_extract(*self._grid(img.shape, o, d), img, np.ascontiguousarray(mute, np.float32),
+                            *self._grid(sub_shape, so, sd), sub, muted)
+        return sub, muted
+
+    def add_data(self, all_data, ishot, shot):
+        """data_rtm_3d::add_data; all_data [nshots][n3][n2][n1]"""
+        L = self._dataimg_sigs()
+        out = np.ascontiguousarray(all_data, np.float32).copy()
+        ns, n3, n2, n1 = out.shape
+        L.ref_add_data(n1, n2, n3, ns, out, ishot, np.ascontiguousarray(shot, np.float32))
+        return out
+
+    def tmute(self, fwd, add, t0, vmute, o1, d1, o2, d2, model, data):
+        """tmute::forward / adjoint on [n5][n4][n3][n2][n1] datasets: (model, data)"""
+        L = self._dataimg_sigs()
+        m = np.ascontiguousarray(model, np.float32).copy()
+        dd = np.ascontiguousarray(data, np.float32).copy()
+        n5, n4, n3, n2, n1 = dd.shape
+        L.ref_tmute(int(fwd), int(add), t0, vmute, n1, o1, d1, n2, o2, d2, n3, n4, n5, m, dd)
+        return m, dd
+
     def cg_solve(self, A, d, niter):
         A = np.ascontiguousarray(A, np.float32)
         m = np.zeros(A.shape[1], np.float32)

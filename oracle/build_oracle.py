@@ -32,16 +32,17 @@ REF_SOURCES = [
     "float_3d.cpp", "my_operator.cpp", "super_vector.cpp", "fd_prop_3d.cpp", "sreg.cpp",
     "sregf.cpp", "oc_float.cpp", "wavefield_insert_3d.cpp", "param_func.cpp", "lin_solver.cpp",
     "combo_oper.cpp", "i_op.cpp", "rtm_zero_op_3d.cpp", "data_rtm_3d.cpp", "image_rtm_3d.cpp",
+    "tmute.cpp",
 ]
 
 
 # Operator methods that are declared bool but fall off their end without a
-# return (Born/deriv_3d.cpp:23,:46, laplac_3d.cpp:44,:96, map_data_3d.cpp:56,:76).
-# Modern g++ treats that as unreachable and the code runs into the next
-# function, so these three files are compiled from their text with
+# return (Born/deriv_3d.cpp:23,:46, laplac_3d.cpp:44,:96, map_data_3d.cpp:56,:76,
+# tmute.cpp:41,:75).  Modern g++ treats that as unreachable and the code runs
+# into the next function, so these files are compiled from their text with
 # `return true;` inserted before each such closing brace (piped to g++, no
 # copy on disk).  Nothing else in the reference text is changed.
-PATCH_RETURNS = {"deriv_3d.cpp", "laplac_3d.cpp", "map_data_3d.cpp"}
+PATCH_RETURNS = {"deriv_3d.cpp", "laplac_3d.cpp", "map_data_3d.cpp", "tmute.cpp"}
 
 
 def _patched_text(src: Path, flags: list[str]) -> bytes:

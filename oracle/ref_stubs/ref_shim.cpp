@@ -8,12 +8,15 @@
 #include "cgstep.h"
 #include "deriv_3d.h"
 #include "float_3d.h"
+#include "data_rtm_3d.h"
 #include "hypercube_float.h"
+#include "image_rtm_3d.h"
 #include "laplac_3d.h"
 #include "lin_solver.h"
 #include "map_data_3d.h"
 #include "sinc_bob.h"
 #include "source_func_3d.h"
+#include "tmute.h"
 #include "vel_fd_3d.h"
 
 namespace {
@@ -206,6 +209,90 @@ int ref_dense_dot_test(const float *A, int nr, int nc, unsigned int seed) {
   dense_op op(A, nr, nc, &mod, &dat);
   srand(seed);
   return op.dot_test(false) ? 1 : 0;
+}
+
+void ref_file_put(const char *tag, int ndim, const int *n, const float *o, const float *d,
+                  const void *data, long nbytes);
+long ref_file_get(const char *tag, void *out, long nbytes);
+
+// ---- image / data vectors (Born/image_rtm_3d.cpp, data_rtm_3d.cpp, tmute.cpp) ----
+
+// image_rtm_3d over a grid (n, o, d): the constructor takes the axes of the
+// velocity model it is given
+static image_rtm_3d *make_image(const int n[3], const float o[3], const float d[3]) {
+  vel_fd_3d *v = new vel_fd_3d();
+  v->fld = new hypercube_float(axes3(n[0], o[0], d[0], n[1], o[1], d[1], n[2], o[2], d[2]));
+  image_rtm_3d *im = new image_rtm_3d((char *)"ref_image", v);
+  delete v;   // deletes fld
+  return im;
+}
+
+// image_rtm_3d::add_image: img (in/out) on grid (n, o, d), sub on (sn, so, sd)
+void ref_image_add(const int n[3], const float o[3], const float d[3], float *img, const int sn[3],
+                   const float so[3], const float sd[3], const float *sub) {
+  image_rtm_3d *im = make_image(n, o, d);
+  const long nn = (long)n[0] * n[1] * n[2], ns = (long)sn[0] * sn[1] * sn[2];
+  memcpy(im->image->vals, img, sizeof(float) * nn);
+  hypercube_float s(axes3(sn[0], so[0], sd[0], sn[1], so[1], sd[1], sn[2], so[2], sd[2]));
+  memcpy(s.vals, sub, sizeof(float) * ns);
+  im->add_image(&s);
+  memcpy(img, im->image->vals, sizeof(float) * nn);
+  delete im;
+}
+
+// image_rtm_3d::extract_sub with the image read from its dataset and the
+// "mute" dataset; also returns write_volume's muted image (image * mute)
+void ref_image_extract(const int n[3], const float o[3], const float d[3], const float *img,
+                       const float *mute, const int sn[3], const float so[3], const float sd[3],
+                       float *sub, float *muted) {
+  const long nn = (long)n[0] * n[1] * n[2], ns = (long)sn[0] * sn[1] * sn[2];
+  ref_file_put("ref_image_src", 3, n, o, d, img, nn * 4);
+  ref_file_put("mute", 3, n, o, d, mute, nn * 4);
+  image_rtm_3d *im = make_image(n, o, d);
+  oc_float src((char *)"ref_image_src");
+  im->set_source_file(&src);
+  float_3d *r = im->extract_sub(axis(sn[0], so[0], sd[0]), axis(sn[1], so[1], sd[1]),
+                                axis(sn[2], so[2], sd[2]));
+  memcpy(sub, r->vals, sizeof(float) * ns);
+  delete r;
+  // write_volume multiplies the image it holds by the mute once more
+  ref_file_put("ref_image_src", 3, n, o, d, img, nn * 4);
+  im->set_source_file(&src);
+  im->write_volume();
+  memcpy(muted, im->image->vals, sizeof(float) * nn);
+  delete im;
+}
+
+// data_rtm_3d::add_data into a dataset of axes (n1, n2, n3, nshots)
+void ref_add_data(int n1, int n2, int n3, int nshots, float *all, int ishot, const float *shot) {
+  const int n[4] = {n1, n2, n3, nshots};
+  const float o[4] = {0.f, 0.f, 0.f, 0.f}, d[4] = {1.f, 1.f, 1.f, 1.f};
+  const long slab = (long)n1 * n2 * n3;
+  ref_file_put("ref_data", 4, n, o, d, all, slab * nshots * 4);
+  data_rtm_3d dat;
+  dat.init_nd(std::vector<axis>{axis(n1), axis(n2), axis(n3), axis(nshots)});
+  oc_float f((char *)"ref_data");
+  dat.set_source_file(&f);
+  hypercube_float h(axes3(n1, 0.f, 1.f, n2, 0.f, 1.f, n3, 0.f, 1.f));
+  memcpy(h.vals, shot, sizeof(float) * slab);
+  dat.add_data(ishot, &h);
+  ref_file_get("ref_data", all, slab * nshots * 4);
+}
+
+// tmute::forward / adjoint on datasets of axes (t, x, n3, n4, n5)
+void ref_tmute(int fwd, int add, float t0, float vmute, int n1, float o1, float d1, int n2, float o2,
+               float d2, int n3, int n4, int n5, float *model, float *data) {
+  const int n[5] = {n1, n2, n3, n4, n5};
+  const float o[5] = {o1, o2, 0.f, 0.f, 0.f}, d[5] = {d1, d2, 1.f, 1.f, 1.f};
+  const long nb = (long)n1 * n2 * n3 * n4 * n5 * 4;
+  ref_file_put("ref_tm_model", 5, n, o, d, model, nb);
+  ref_file_put("ref_tm_data", 5, n, o, d, data, nb);
+  oc_float m((char *)"ref_tm_model"), dd((char *)"ref_tm_data");
+  tmute op(t0, vmute, &m, &dd);
+  if (fwd) op.forward(add != 0, &m, &dd);
+  else op.adjoint(add != 0, &m, &dd);
+  ref_file_get("ref_tm_model", model, nb);
+  ref_file_get("ref_tm_data", data, nb);
 }
 
 }  // extern "C"

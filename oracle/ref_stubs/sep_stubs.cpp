@@ -144,6 +144,18 @@ int sep_put_data_axis_par(const char *tag, int *i, int *n, float *o, float *d, c
 
 void initpar(int, char **) {}
 
+// oc_float::make_temp (Born/oc_float.cpp:406-412) names temporary datasets
+// with mkstemp, which would create files in the working directory: the
+// checker's datasets live in memory, so this library's own calls get a
+// unique name and no file (no descriptor is returned; the reference ignores it).
+int mkstemp(char *tmpl) {
+  static unsigned long long counter = 0;
+  const size_t n = strlen(tmpl);
+  unsigned long long v = ++counter;
+  for (size_t i = n; i > 0 && tmpl[i - 1] == 'X'; i--, v /= 10) tmpl[i - 1] = (char)('0' + v % 10);
+  return -1;
+}
+
 // ---- registry access for the checker ----
 void ref_reset(void) { g_files.clear(); g_params.clear(); }
 

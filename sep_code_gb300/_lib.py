@@ -68,6 +68,13 @@ def _load() -> C.CDLL:
     L.sepx_snapshot_bytes.restype = C.c_longlong
     L.sepx_dot_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_double)]
     L.sepx_dot_f32.restype = C.c_int
+    # image / data vectors on the device (device pointers)
+    vp = C.c_void_p
+    L.sepx_image_add_window.argtypes = [vp, i, i, i, i, i, i, vp, i, i, i]
+    L.sepx_image_extract_window.argtypes = [vp, vp, i, i, i, i, i, i, vp, i, i, i]
+    L.sepx_tmute.argtypes = [i, i, f, f, i, f, f, i, f, f, C.c_longlong, vp, vp]
+    for name in ("sepx_image_add_window", "sepx_image_extract_window", "sepx_tmute"):
+        getattr(L, name).restype = C.c_int
     # host set-up math
     L.sepx_host_sinc_table.argtypes = [i, i, F32P]
     L.sepx_host_glibc_rand_sequence.argtypes = [C.c_uint, i, I32P]

@@ -43,5 +43,13 @@ cudaError_t launch_data_from_traces(const float *trc, int nrec, int rnx, int nt,
                                     float *data, cudaStream_t st);
 cudaError_t launch_traces_from_data(const float *data, int nrec, int rnx, int nt, int ntrace,
                                     float dt, float *trc, cudaStream_t st);
+cudaError_t launch_window_add(float *img, int n1, int n2, int n3, const float *sub, int s1, int s2,
+                              int s3, int f1, int f2, int f3, cudaStream_t st);
+cudaError_t launch_window_extract(const float *img, const float *mute, int n1, int n2, int n3,
+                                  float *sub, int s1, int s2, int s3, int f1, int f2, int f3,
+                                  cudaStream_t st);
+cudaError_t launch_tmute(const float *in, float *out, int add, float t0, float vmute, int n1,
+                         float o1, float d1, int n2, float o2, float d2, long long nrep,
+                         cudaStream_t st);
 
 }  // namespace sepx

@@ -969,6 +969,43 @@ int sepx_op_data_to_traces(const float *data, int nt, float dt) {
   return 0;
 }
 
+// ------------------------------------------------------------ data / image vectors
+int sepx_image_add_window(float *img, int n1, int n2, int n3, int f1, int f2, int f3,
+                          const float *sub, int s1, int s2, int s3) {
+  RET(need_device());
+  if (!img || !sub) return fail("image_add_window: NULL buffer");
+  if (n1 < 1 || n2 < 1 || n3 < 1 || s1 < 0 || s2 < 0 || s3 < 0)
+    return fail("image_add_window: invalid sizes");
+  if ((long long)s1 * s2 * s3 == 0) return 0;
+  CKL(launch_window_add(img, n1, n2, n3, sub, s1, s2, s3, f1, f2, f3, G.stream));
+  return 0;
+}
+
+int sepx_image_extract_window(const float *img, const float *mute, int n1, int n2, int n3, int f1,
+                              int f2, int f3, float *sub, int s1, int s2, int s3) {
+  RET(need_device());
+  if (!img || !sub) return fail("image_extract_window: NULL buffer");
+  if (n1 < 1 || n2 < 1 || n3 < 1 || s1 < 0 || s2 < 0 || s3 < 0)
+    return fail("image_extract_window: invalid sizes");
+  if ((long long)s1 * s2 * s3 == 0) return 0;
+  CKL(launch_window_extract(img, mute, n1, n2, n3, sub, s1, s2, s3, f1, f2, f3, G.stream));
+  return 0;
+}
+
+int sepx_tmute(int adj, int add, float t0, float vmute, int n1, float o1, float d1, int n2, float o2,
+               float d2, long long nrep, float *model, float *data) {
+  RET(need_device());
+  if (!model || !data) return fail("tmute: NULL buffer");
+  if (n1 < 1 || n2 < 1 || nrep < 0) return fail("tmute: invalid sizes");
+  if (!(vmute != 0.f) || !(d1 != 0.f)) return fail("tmute: vmute and d1 must be non-zero");
+  if (nrep == 0) return 0;
+  if (adj)
+    CKL(launch_tmute(data, model, add, t0, vmute, n1, o1, d1, n2, o2, d2, nrep, G.stream));
+  else
+    CKL(launch_tmute(model, data, add, t0, vmute, n1, o1, d1, n2, o2, d2, nrep, G.stream));
+  return 0;
+}
+
 // ------------------------------------------------------------ device vectors (BLAS-1)
 int sepx_vec_alloc(float **p, long long n) {
   RET(need_device());

@@ -100,6 +100,108 @@ __global__ void traces_from_data_kernel(const float *__restrict__ data, int nrec
   }
 }
 
+// ---- data / image vectors kept on the device (the reference keeps them in
+// out-of-core files and loops over them on the host) ----
+
+// image_rtm_3d::add_image (Born/image_rtm_3d.cpp:24-49): img[j + f] += sub[j]
+// for every sub cell whose shifted position lies inside img.  One block row
+// per (i2, i3) row of sub, consecutive threads along axis 1.
+__global__ void window_add_kernel(float *__restrict__ img, int n1, int n2, int n3,
+                                  const float *__restrict__ sub, int s1, int s2, int s3, int f1,
+                                  int f2, int f3) {
+  const long long rows = (long long)s2 * s3;
+  for (long long r = blockIdx.y; r < rows; r += gridDim.y) {
+    const int i2 = (int)(r % s2), i3 = (int)(r / s2);
+    const int j2 = i2 + f2, j3 = i3 + f3;
+    if (j2 < 0 || j2 >= n2 || j3 < 0 || j3 >= n3) continue;   // uniform for the block
+    float *orow = img + (long long)n1 * (j2 + (long long)n2 * j3);
+    const float *irow = sub + (long long)s1 * r;
+    for (int i1 = blockIdx.x * blockDim.x + threadIdx.x; i1 < s1; i1 += gridDim.x * blockDim.x) {
+      const int j1 = i1 + f1;
+      if (j1 >= 0 && j1 < n1) orow[j1] = __fadd_rn(orow[j1], irow[i1]);
+    }
+  }
+}
+
+// image_rtm_3d::extract_sub (Born/image_rtm_3d.cpp:52-90): sub[j] =
+// img[j + f] * mute[j + f] (mute may be NULL: a unit mute), 0 where the
+// shifted position lies outside img.
+__global__ void window_extract_kernel(const float *__restrict__ img, const float *__restrict__ mute,
+                                      int n1, int n2, int n3, float *__restrict__ sub, int s1,
+                                      int s2, int s3, int f1, int f2, int f3) {
+  const long long rows = (long long)s2 * s3;
+  for (long long r = blockIdx.y; r < rows; r += gridDim.y) {
+    const int i2 = (int)(r % s2), i3 = (int)(r / s2);
+    const int j2 = i2 + f2, j3 = i3 + f3;
+    const bool row_in = j2 >= 0 && j2 < n2 && j3 >= 0 && j3 < n3;
+    const long long ro = (long long)n1 * (j2 + (long long)n2 * j3);
+    float *orow = sub + (long long)s1 * r;
+    for (int i1 = blockIdx.x * blockDim.x + threadIdx.x; i1 < s1; i1 += gridDim.x * blockDim.x) {
+      const int j1 = i1 + f1;
+      float v = 0.f;
+      if (row_in && j1 >= 0 && j1 < n1) {
+        v = img[ro + j1];
+        if (mute) v = __fmul_rn(v, mute[ro + j1]);
+      }
+      orow[i1] = v;
+    }
+  }
+}
+
+// tmute (Born/tmute.cpp:4-76): out[rep][i2][i1] (+)= in[...] for i1 >= the
+// first unmuted sample (int)((t_0 + (o2 + d2 i2) / vmute - o1) / d1) of
+// trace i2, computed in single precision exactly as the reference does; a
+// start before the first sample is taken as 0.  Without `add` the samples
+// before the start are zeroed.
+__global__ void tmute_kernel(const float *__restrict__ in, float *__restrict__ out, int add,
+                             float t0, float vmute, int n1, float o1, float d1, int n2, float o2,
+                             float d2, long long nrep) {
+  const long long rows = (long long)n2 * nrep;
+  for (long long r = blockIdx.y; r < rows; r += gridDim.y) {
+    const int i2 = (int)(r % n2);
+    const float tr = __fadd_rn(t0, __fdiv_rn(__fadd_rn(o2, __fmul_rn(d2, (float)i2)), vmute));
+    const float sf = __fdiv_rn(__fsub_rn(tr, o1), d1);
+    const int start = (sf >= (float)n1) ? n1 : max(0, __float2int_rz(sf));
+    const float *irow = in + (long long)n1 * r;
+    float *orow = out + (long long)n1 * r;
+    for (int i1 = blockIdx.x * blockDim.x + threadIdx.x; i1 < n1; i1 += gridDim.x * blockDim.x) {
+      float v = add ? orow[i1] : 0.f;
+      if (i1 >= start) v = __fadd_rn(v, irow[i1]);
+      orow[i1] = v;
+    }
+  }
+}
+
+static dim3 rows_grid(int n1, long long rows) {
+  // about 16 resident rows of 256 threads per SM on 152 SMs, x covering a row
+  const int gx = (n1 + 255) / 256 < 8 ? (n1 + 255) / 256 : 8;
+  long long gy = rows < 2432 ? rows : 2432;
+  return dim3(gx < 1 ? 1 : gx, (unsigned)(gy < 1 ? 1 : gy));
+}
+
+cudaError_t launch_window_add(float *img, int n1, int n2, int n3, const float *sub, int s1, int s2,
+                              int s3, int f1, int f2, int f3, cudaStream_t st) {
+  window_add_kernel<<<rows_grid(s1, (long long)s2 * s3), 256, 0, st>>>(img, n1, n2, n3, sub, s1, s2,
+                                                                       s3, f1, f2, f3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_window_extract(const float *img, const float *mute, int n1, int n2, int n3,
+                                  float *sub, int s1, int s2, int s3, int f1, int f2, int f3,
+                                  cudaStream_t st) {
+  window_extract_kernel<<<rows_grid(s1, (long long)s2 * s3), 256, 0, st>>>(img, mute, n1, n2, n3, sub,
+                                                                           s1, s2, s3, f1, f2, f3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tmute(const float *in, float *out, int add, float t0, float vmute, int n1,
+                         float o1, float d1, int n2, float o2, float d2, long long nrep,
+                         cudaStream_t st) {
+  tmute_kernel<<<rows_grid(n1, (long long)n2 * nrep), 256, 0, st>>>(in, out, add, t0, vmute, n1, o1,
+                                                                    d1, n2, o2, d2, nrep);
+  return cudaGetLastError();
+}
+
 static int grid_of(long long n) {
   long long g = (n + 255) / 256;
   return (int)(g < 4096 ? (g < 1 ? 1 : g) : 4096);

@@ -337,7 +337,12 @@ my_vector *lin_solver::init_rr(my_vector *data, my_operator *op, my_vector *m0) 
 bool lin_solver::solve(int niter) {
   const auto t0 = std::chrono::steady_clock::now();
   double prev = rr->dot(rr);
+  const double rr0 = prev;
   bool use_dir = dir != nullptr;
+  if (dir_policy == SEPX_DIR_ADAPTIVE && probe_every < 1)
+    throw std::runtime_error("probe_every must be at least 1");
+  double gain_plain = -1.0;   // fraction of rr.rr removed by the latest plain step
+  int plain_run = 0;
   for (int iter = 0; iter < niter; iter++) {
     oper->adjoint(false, g, rr, iter);
     if (use_dir) {
@@ -349,16 +354,32 @@ bool lin_solver::solve(int niter) {
     double val = 0;
     const bool valid = st->step_it(iter, m, g, rr, gg, &val);
     if (!valid) return false;
-    // plain CG is the fallback: once a preconditioned step lowers rr.rr by
-    // less than the ratio allows, the remaining iterations use plain g
-    if (use_dir && fallback_ratio > 0 && val > fallback_ratio * prev) {
-      use_dir = false;
-      fallback_iter = iter;
+    used_dir.push_back(use_dir ? 1 : 0);
+    const double gain = prev > 0 ? 1.0 - val / prev : 0.0;
+    bool next = use_dir;
+    if (dir != nullptr && dir_policy == SEPX_DIR_ADAPTIVE) {
+      if (use_dir) {
+        // keep the preconditioned direction while it removes at least the
+        // fraction the latest plain step removed
+        next = gain_plain < 0 ? !(fallback_ratio > 0 && val > fallback_ratio * prev)
+                              : gain >= gain_plain;
+        plain_run = 0;
+      } else {
+        gain_plain = gain;
+        next = ++plain_run >= probe_every;
+      }
+    } else if (use_dir && fallback_ratio > 0 && val > fallback_ratio * prev) {
+      // plain CG is the fallback: once a preconditioned step lowers rr.rr by
+      // less than the ratio allows, the remaining iterations use plain g
+      next = false;
     }
+    if (use_dir && !next && fallback_iter < 0) fallback_iter = iter;
+    use_dir = next;
     prev = val;
     resid.push_back(val);
     seconds.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
     if (verb > 0) fprintf(stderr, "iter %d residual %g\n", iter, val);
+    if (target > 0 && val <= target * target * rr0) break;
   }
   return true;
 }
@@ -682,4 +703,130 @@ int sepx_lsrtm(sepx_op_handle h, const float *data, int niter, float *model, dou
   }
 }
 
+int sepx_lsrtm_ex(sepx_op_handle h, const float *data, int niter, const sepx_lsrtm_opts *opts,
+                  float *model, double *resid, double *seconds, int *used_dir, int *iters_done) {
+  try {
+    if (!opts) return sepx::set_error("lsrtm_ex: opts is NULL");
+    if (opts->policy != SEPX_DIR_FALLBACK && opts->policy != SEPX_DIR_ADAPTIVE)
+      return sepx::set_error("lsrtm_ex: unknown direction policy %d", opts->policy);
+    auto *b = static_cast<op_box *>(h);
+    b->data->upload(data);
+    cgstep st;
+    simple_solver solv(&st, b->data.get(), b->op.get());
+    solv.dir = opts->dir;
+    solv.dir_ctx = opts->dir_ctx;
+    solv.dir_policy = opts->policy;
+    solv.fallback_ratio = opts->fallback_ratio;
+    solv.probe_every = opts->probe_every;
+    solv.target = opts->target;
+    solv.solve(niter);
+    std::unique_ptr<my_vector> mod(solv.return_model());
+    hf(mod.get())->download(model);
+    const size_t done = solv.resid.size();
+    for (size_t i = 0; i < (size_t)niter; i++) {
+      const bool ran = i < done;
+      if (resid) resid[i] = ran ? solv.resid[i] : -1.0;
+      if (seconds) seconds[i] = ran ? solv.seconds[i] : -1.0;
+      if (used_dir) used_dir[i] = ran ? solv.used_dir[i] : -1;
+    }
+    if (iters_done) *iters_done = (int)done;
+    return 0;
+  } catch (const std::exception &e) {
+    return sepx::set_error("lsrtm_ex: %s", e.what());
+  }
+}
+
 }  // extern "C"
+
+// ------------------------------------------------------------------ tmute, image, data
+namespace {
+// first cell of a window in the grid of `out`, as image_rtm_3d computes it
+// (Born/image_rtm_3d.cpp:33-35): (int)((o_in - o_out) / d_out) in float
+int window_offset(const axis &in, const axis &out) { return (int)((in.o - out.o) / out.d); }
+
+void need3(const hypercube_float *h, const char *what) {
+  if (h->axes.size() < 3) throw std::runtime_error(std::string(what) + ": needs three axes");
+}
+}  // namespace
+
+tmute::tmute(float t, float v, my_vector *mod, my_vector *dat) : t_0(t), vmute(v) {
+  set_domain(mod);
+  set_range(dat);
+}
+
+static void tmute_apply(bool adj, bool add, float t0, float vm, my_vector *model, my_vector *data) {
+  auto *m = hf(model), *d = hf(data);
+  if (m->n123 != d->n123 || d->axes.size() < 2) throw std::runtime_error("tmute: shapes differ");
+  const axis a1 = d->get_axis(1), a2 = d->get_axis(2);
+  const long long nrep = d->n123 / ((long long)a1.n * a2.n);
+  ck(sepx_tmute(adj ? 1 : 0, add ? 1 : 0, t0, vm, a1.n, a1.o, a1.d, a2.n, a2.o, a2.d, nrep, m->vals,
+                d->vals),
+     "tmute");
+}
+
+bool tmute::forward(bool add, my_vector *model, my_vector *data, int) {
+  tmute_apply(false, add, t_0, vmute, model, data);
+  return true;
+}
+
+bool tmute::adjoint(bool add, my_vector *model, my_vector *data, int) {
+  tmute_apply(true, add, t_0, vmute, model, data);
+  return true;
+}
+
+image_rtm_3d::image_rtm_3d(const std::vector<axis> &axes) {
+  if (axes.size() != 3) throw std::runtime_error("image_rtm_3d: needs three axes");
+  image = new hypercube_float(axes);
+}
+
+image_rtm_3d::~image_rtm_3d() {
+  delete image;
+  delete mute;
+}
+
+void image_rtm_3d::set_mute(const hypercube_float &m) {
+  if (m.n123 != image->n123) throw std::runtime_error("image_rtm_3d: mute shape differs");
+  if (!mute) mute = new hypercube_float(image->axes);
+  ck(sepx_vec_copy(mute->vals, m.vals, m.n123), "set_mute");
+}
+
+void image_rtm_3d::add_image(const hypercube_float *img) {
+  need3(img, "add_image");
+  const axis o1 = get_axis(1), o2 = get_axis(2), o3 = get_axis(3);
+  const axis i1 = img->get_axis(1), i2 = img->get_axis(2), i3 = img->get_axis(3);
+  ck(sepx_image_add_window(image->vals, o1.n, o2.n, o3.n, window_offset(i1, o1),
+                           window_offset(i2, o2), window_offset(i3, o3), img->vals, i1.n, i2.n,
+                           i3.n),
+     "add_image");
+}
+
+hypercube_float *image_rtm_3d::extract_sub(axis a1, axis a2, axis a3) const {
+  const axis o1 = get_axis(1), o2 = get_axis(2), o3 = get_axis(3);
+  std::unique_ptr<hypercube_float> sub(new hypercube_float({a1, a2, a3}));
+  ck(sepx_image_extract_window(image->vals, mute ? mute->vals : nullptr, o1.n, o2.n, o3.n,
+                               window_offset(a1, o1), window_offset(a2, o2), window_offset(a3, o3),
+                               sub->vals, a1.n, a2.n, a3.n),
+     "extract_sub");
+  return sub.release();
+}
+
+void image_rtm_3d::write_volume() {
+  if (mute) image->mult(mute);
+}
+
+data_rtm_3d::data_rtm_3d(const std::vector<axis> &ax) : hypercube_float(ax) {
+  if (ax.size() < 3) throw std::runtime_error("data_rtm_3d: needs (t, x, y[, shots]) axes");
+}
+
+int data_rtm_3d::nshots() const {
+  int n = 1;
+  for (size_t i = 3; i < axes.size(); i++) n *= axes[i].n;
+  return n;
+}
+
+void data_rtm_3d::add_data(int ishot, const hypercube_float *dat) {
+  const long long slab = (long long)axes[0].n * axes[1].n * axes[2].n;
+  if (ishot < 0 || ishot >= nshots()) throw std::runtime_error("add_data: shot out of range");
+  if (dat->n123 != slab) throw std::runtime_error("add_data: the shot's size differs");
+  ck(sepx_vec_add(vals + (long long)ishot * slab, dat->vals, slab), "add_data");
+}

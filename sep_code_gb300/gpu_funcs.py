@@ -143,6 +143,23 @@ def snapshot_bytes(nt, js, prec) -> int:
     return int(lib.sepx_snapshot_bytes(nt, js, SNAP_PREC[prec]))
 
 
+# ---- image / data vectors kept on the device (device pointers, context stream) ----
+def image_add_window(img_ptr, n, f, sub_ptr, s) -> None:
+    """image_rtm_3d::add_image: img (n1, n2, n3) cell j + f += sub (s1, s2, s3) cell j"""
+    check(lib.sepx_image_add_window(img_ptr, *n, *f, sub_ptr, *s), "image_add_window")
+
+
+def image_extract_window(img_ptr, mute_ptr, n, f, sub_ptr, s) -> None:
+    """image_rtm_3d::extract_sub: sub cell j = (img * mute) cell j + f, 0 outside"""
+    check(lib.sepx_image_extract_window(img_ptr, mute_ptr, *n, *f, sub_ptr, *s), "image_extract_window")
+
+
+def tmute(adj, add, t0, vmute, n1, o1, d1, n2, o2, d2, nrep, model_ptr, data_ptr) -> None:
+    """tmute::forward (adj=False) / adjoint on [nrep][n2][n1] traces"""
+    check(lib.sepx_tmute(int(adj), int(add), t0, vmute, n1, o1, d1, n2, o2, d2, nrep, model_ptr,
+                         data_ptr), "tmute")
+
+
 def synchronize() -> None:
     check(lib.sepx_synchronize(), "synchronize")
 

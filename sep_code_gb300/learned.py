@@ -190,24 +190,32 @@ def lsrtm_survey(n: int = 384, nt: int = 3000, nshots: int = 4, d: float = 12.5,
 
 
 def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 4,
-                  snap_prec: str = "bf16", fallback_ratio: float = 0.9, verbose: bool = False) -> dict:
+                  snap_prec: str = "bf16", fallback_ratio: float = 0.9, verbose: bool = False,
+                  policies=("fallback",), probe_every: int = 8, target: float = 0.0) -> dict:
     """Plain simple_solver + cgstep against the same solver with the learned
-    direction, on data d = L m_true of the survey's reflectivity."""
+    direction (one run per direction policy), on data d = L m_true of the
+    survey's reflectivity.  target > 0 stops every run at that relative data
+    residual (niter caps it).  "learned" holds the first policy's run."""
     op = RtmOperator(s, mode="linear", snap_js=snap_js, snap_prec=snap_prec)
+    runs = {}
     try:
         t0 = time.perf_counter()
         d = op.forward(s.refl)
         t_fwd = time.perf_counter() - t0
         dd = float(np.dot(d.astype(np.float64).ravel(), d.astype(np.float64).ravel()))
-        m_plain, r_plain, s_plain = op.lsrtm(d, niter)
+        m_plain, r_plain, s_plain = op.lsrtm(d, niter, target=target)
         if verbose:
             print("plain", np.sqrt(r_plain / dd), s_plain, flush=True)
         net = load_network() if net is None else net
-        hook = UNetDirection(net, op.model_shape)
-        m_nn, r_nn, s_nn = op.lsrtm(d, niter, direction=hook, fallback_ratio=fallback_ratio)
-        fb_iter = op.fallback_iter
-        if verbose:
-            print("learned", np.sqrt(r_nn / dd), s_nn, flush=True)
+        for pol in policies:
+            hook = UNetDirection(net, op.model_shape)
+            m_nn, r_nn, s_nn = op.lsrtm(d, niter, direction=hook, fallback_ratio=fallback_ratio,
+                                        policy=pol, probe_every=probe_every, target=target)
+            used = op.used_dir
+            runs[pol] = (m_nn, r_nn, s_nn, hook.seconds, hook.calls, op.fallback_iter,
+                         None if used is None else used.tolist())
+            if verbose:
+                print("learned", pol, np.sqrt(r_nn / dd), s_nn, flush=True)
     finally:
         op.close()
 
@@ -218,20 +226,35 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
         hit = np.nonzero(res <= level)[0]
         return float(secs[hit[0]]) if len(hit) else None
 
-    rp, rn = np.sqrt(r_plain / dd), np.sqrt(r_nn / dd)
+    rp = np.sqrt(r_plain / dd)
     final_plain = float(rp[-1])
+    by_policy = {}
+    for pol, (m_nn, r_nn, s_nn, dsec, dcalls, fb_iter, used) in runs.items():
+        rn = np.sqrt(r_nn / dd)
+        by_policy[pol] = {
+            "rel_residual": rn.tolist(), "seconds": s_nn.tolist(),
+            "direction_seconds": dsec, "direction_calls": dcalls,
+            "fallback_ratio": fallback_ratio, "probe_every": probe_every if pol == "adaptive" else None,
+            "plain_g_from_iteration": fb_iter + 1 if fb_iter >= 0 else None,
+            "used_direction": used,
+            "time_to_1e-2": t_to(rn, s_nn, 1e-2),
+            "time_to_plain_final_residual": t_to(rn, s_nn, final_plain),
+            "image_rel_l2_vs_plain_cg": rel(m_nn, m_plain),
+            "image_rel_l2_vs_true": rel(m_nn, s.refl),
+        }
+    first = by_policy[policies[0]]
     return {
-        "workload": s.name, "iterations": niter, "store": f"{snap_prec} every {snap_js} steps",
+        "workload": s.name, "iterations": niter, "target": target or None,
+        "store": f"{snap_prec} every {snap_js} steps",
         "seconds_data_generation": t_fwd,
         "plain": {"rel_residual": rp.tolist(), "seconds": s_plain.tolist()},
-        "learned": {"rel_residual": rn.tolist(), "seconds": s_nn.tolist(),
-                    "direction_seconds": hook.seconds, "direction_calls": hook.calls,
-                    "fallback_ratio": fallback_ratio, "plain_g_from_iteration": fb_iter + 1 if fb_iter >= 0 else None},
-        "time_to_1e-2": {"plain": t_to(rp, s_plain, 1e-2), "learned": t_to(rn, s_nn, 1e-2)},
+        "learned": first,
+        "learned_by_policy": by_policy,
+        "time_to_1e-2": {"plain": t_to(rp, s_plain, 1e-2), "learned": first["time_to_1e-2"]},
         "time_to_plain_final_residual": {"plain": float(s_plain[-1]),
-                                         "learned": t_to(rn, s_nn, final_plain)},
-        "image_rel_l2_vs_plain_cg": {"learned_final": rel(m_nn, m_plain)},
-        "image_rel_l2_vs_true": {"plain": rel(m_plain, s.refl), "learned": rel(m_nn, s.refl)},
+                                         "learned": first["time_to_plain_final_residual"]},
+        "image_rel_l2_vs_plain_cg": {"learned_final": first["image_rel_l2_vs_plain_cg"]},
+        "image_rel_l2_vs_true": {"plain": rel(m_plain, s.refl), "learned": first["image_rel_l2_vs_true"]},
     }
 
 
@@ -255,6 +278,9 @@ def main(argv=None):
     c.add_argument("--iters", type=int, default=20)
     c.add_argument("--weights", default=str(WEIGHTS))
     c.add_argument("--out", default=None)
+    c.add_argument("--policies", default="fallback", help="comma list of fallback,adaptive")
+    c.add_argument("--probe-every", type=int, default=8)
+    c.add_argument("--target", type=float, default=0.0)
     a = p.parse_args(argv)
     if a.cmd == "train":
         t0 = time.perf_counter()
@@ -269,7 +295,9 @@ def main(argv=None):
                           "seconds_training": t2 - t1, "epochs": a.epochs, "loss": hist}))
     else:
         s = lsrtm_survey(a.n, a.nt, a.shots)
-        res = lsrtm_compare(s, a.iters, net=load_network(a.weights), verbose=True)
+        res = lsrtm_compare(s, a.iters, net=load_network(a.weights), verbose=True,
+                            policies=tuple(a.policies.split(",")), probe_every=a.probe_every,
+                            target=a.target)
         txt = json.dumps(res)
         print(txt)
         if a.out:

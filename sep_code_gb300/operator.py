@@ -42,6 +42,18 @@ lib.sepx_rtm_op_dot_test.argtypes = [C.c_void_p, C.c_ulonglong, _F64P]
 lib.sepx_lsrtm.argtypes = [C.c_void_p, _F32P, C.c_int, _F32P, _F64P, _F64P, C.c_void_p, C.c_void_p,
                            C.c_double, C.POINTER(C.c_int)]
 
+
+class LsrtmOpts(C.Structure):
+    """sepx_lsrtm_opts (include/sepx_ops.h)"""
+    _fields_ = [("dir", C.c_void_p), ("dir_ctx", C.c_void_p), ("policy", C.c_int),
+                ("fallback_ratio", C.c_double), ("probe_every", C.c_int), ("target", C.c_double)]
+
+
+_I32P = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+lib.sepx_lsrtm_ex.argtypes = [C.c_void_p, _F32P, C.c_int, C.POINTER(LsrtmOpts), _F32P, _F64P, _F64P,
+                              _I32P, C.POINTER(C.c_int)]
+POLICIES = {"fallback": 0, "adaptive": 1}
+
 MODES = {"reference": 0, "linear": 1}
 PREC = {"f32": 0, "bf16": 1, "f16": 2}
 
@@ -96,21 +108,40 @@ class RtmOperator:
         self._chk(lib.sepx_rtm_op_dot_test(self.h, seed, out))
         return out
 
-    def lsrtm(self, data, niter: int, direction=None, fallback_ratio: float = 0.0):
+    def lsrtm(self, data, niter: int, direction=None, fallback_ratio: float = 0.0,
+              policy: str = "fallback", probe_every: int = 8, target: float = 0.0):
         """simple_solver + cgstep; ``direction(g_ptr, n)`` may precondition the
-        search direction in place (device pointer); with fallback_ratio > 0 the
-        solver returns to plain g once a preconditioned step lowers rr.rr by
-        less than that ratio (``self.fallback_iter`` records where).  Returns
-        (model, rr.rr per iteration, seconds per iteration)."""
+        search direction in place (device pointer).  policy "fallback": with
+        fallback_ratio > 0 the solver returns to plain g once a preconditioned
+        step lowers rr.rr by less than that ratio (``self.fallback_iter``
+        records where); "adaptive": the preconditioned direction is kept while
+        its steps remove at least the fraction of rr.rr the latest plain step
+        removed, and retried every ``probe_every`` plain iterations.  target >
+        0 stops once the residual falls to that fraction of the initial one.
+        Returns (model, rr.rr per iteration, seconds per iteration) for the
+        iterations run; ``self.used_dir`` marks the preconditioned ones."""
         model = np.zeros(self.model_shape, np.float32)
         resid = np.zeros(niter, np.float64)
         secs = np.zeros(niter, np.float64)
+        used = np.zeros(niter, np.int32)
         cb = None
         if direction is not None:
             cb = DIRECTION_FN(lambda ctx, g, n: int(direction(g, n) or 0))
-        fb = C.c_int(-1)
-        self._chk(lib.sepx_lsrtm(self.h, np.ascontiguousarray(data, np.float32), niter, model, resid, secs,
-                                 C.cast(cb, C.c_void_p) if cb else None, None, fallback_ratio,
-                                 C.byref(fb)))
-        self.fallback_iter = fb.value
-        return model, resid, secs
+        done = C.c_int(0)
+        if policy == "fallback" and target <= 0:
+            fb = C.c_int(-1)
+            self._chk(lib.sepx_lsrtm(self.h, np.ascontiguousarray(data, np.float32), niter, model, resid,
+                                     secs, C.cast(cb, C.c_void_p) if cb else None, None, fallback_ratio,
+                                     C.byref(fb)))
+            self.fallback_iter = fb.value
+            self.used_dir = None
+            return model, resid, secs
+        opts = LsrtmOpts(C.cast(cb, C.c_void_p) if cb else None, None, POLICIES[policy], fallback_ratio,
+                         probe_every, target)
+        self._chk(lib.sepx_lsrtm_ex(self.h, np.ascontiguousarray(data, np.float32), niter, C.byref(opts),
+                                    model, resid, secs, used, C.byref(done)))
+        k = done.value
+        self.used_dir = used[:k].copy()
+        off = np.nonzero(self.used_dir == 0)[0] if cb else []
+        self.fallback_iter = int(off[0]) - 1 if len(off) else -1
+        return model, resid[:k], secs[:k]

@@ -39,3 +39,47 @@ def test_direction_hook_is_finite_and_in_place():
     torch.cuda.synchronize()
     assert torch.isfinite(g).all()
     assert not torch.equal(g, before)
+
+
+def _replay_adaptive(rr, rr0, used, ratio, probe):
+    """the SEPX_DIR_ADAPTIVE rule applied to the recorded residual energies"""
+    want, cur, gain_plain, run, prev = [], 1, -1.0, 0, rr0
+    for v in rr:
+        want.append(cur)
+        gain = 1.0 - v / prev
+        if cur:
+            cur = int(not (ratio > 0 and v > ratio * prev)) if gain_plain < 0 else int(gain >= gain_plain)
+            run = 0
+        else:
+            gain_plain = gain
+            run += 1
+            cur = int(run >= probe)
+        prev = v
+    return want
+
+
+def test_adaptive_direction_policy_and_target_stop():
+    """SEPX_DIR_ADAPTIVE follows its rule iteration by iteration (checked by
+    replaying it on the recorded residuals), keeps the residual
+    non-increasing, and a target residual stops the solver at the first
+    iteration that reaches it."""
+    from sep_code_gb300 import learned as Lr
+    from sep_code_gb300.operator import RtmOperator
+    s = Lr.lsrtm_survey(n=64, nt=1000, nshots=1, seed=97)
+    op = RtmOperator(s, mode="linear", snap_js=4, snap_prec="f32")
+    try:
+        d = op.forward(s.refl)
+        dd = float(np.dot(d.astype(np.float64).ravel(), d.astype(np.float64).ravel()))
+        hook = Lr.UNetDirection(Lr.load_network(), op.model_shape)
+        _, rr, _ = op.lsrtm(d, 10, direction=hook, fallback_ratio=0.9, policy="adaptive", probe_every=2)
+        used = op.used_dir.tolist()
+        assert len(rr) == 10 and np.all(np.diff(rr) <= 1e-12 * dd)
+        assert used[0] == 1 and 0 in used
+        assert used == _replay_adaptive(rr, dd, used, 0.9, 2)
+        # the plain run stopped by a target taken from its own 6th iteration
+        _, rp, _ = op.lsrtm(d, 10)
+        tgt = float(np.sqrt(rp[5] / dd)) * (1 + 1e-9)
+        _, rs, _ = op.lsrtm(d, 10, target=tgt)
+        assert len(rs) == 6 and np.allclose(rs, rp[:6], rtol=0, atol=0)
+    finally:
+        op.close()

@@ -41,12 +41,12 @@ def _declared(header):
 
 
 @pytest.mark.parametrize("header", ["sepx.h", "sepx_host.h", "sepx_ops.h", "sepx_batch.h",
-                                    "sepx_unet.h"])
+                                    "sepx_unet.h", "sepx_sepio.h"])
 def test_library_exports_every_declared_symbol(header):
     from sep_code_gb300 import LIB_PATH
     lib = C.CDLL(str(LIB_PATH))
     names = _declared(header)
-    assert len(names) >= 5
+    assert len(names) >= 5 or (header == "sepx_sepio.h" and len(names) == 5)
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
