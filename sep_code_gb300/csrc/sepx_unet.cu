@@ -15,8 +15,10 @@
 // N = output channels (16..128), K = taps x input channels (chunks of 64);
 // weight gradient  M = taps x input channels (tiles of 128), N = output
 // channels, K = voxels (chunks of 64, split over CTAs, FP32 atomics).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdint>
 
@@ -245,6 +247,193 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
         }
       }
     }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
+// Forward (and data-gradient) 3x3x3 convolution from a staged input halo.
+// Output tile: 128 voxels = 16 rows (y) x 8 columns (x) of one z plane of one
+// volume.  Its input halo -- 3 planes x 18 rows x 10 columns, every channel --
+// is brought into shared memory by TMA once (zero fill outside the volume),
+// channel group g (8 channels, 16 B) at g * kHaloGS bytes, voxel (z, y, x) of
+// the halo at ((z * 18 + y) * 10 + x) * 16 within it.  For tap (dz, dy, dx)
+// the A operand (M = 128 voxels, K = 16 channels) is a K-major no-swizzle view
+// of that block: core matrix = 8 consecutive x of one row (128 B contiguous),
+// M-group stride 160 B (next row), K-group stride kHaloGS (next 8 channels),
+// start shifted by the tap.  So every input byte crosses L2 once per tile
+// instead of once per tap.  All packed weights of the layer stay in shared
+// memory; B for (tap t, channels 16s..16s+15) starts at K group t*cin/8 + 2s.
+// One thread issues the 27 * cin/16 MMAs (M128, N = np, K16) into tensor
+// memory; the CTA walks tiles (persistent), prefetching the next tile's halo
+// into the other of two buffers while the current one is computed.
+// ---------------------------------------------------------------------------
+constexpr int kHaloX = 10, kHaloY = 18, kHaloZ = 3;
+constexpr int kHaloGS = 8704;   // bytes per channel group (8640 rounded up to 128)
+constexpr int kTileY = 16, kTileX = 8;
+
+struct HaloArgs {
+  int nb, D, H, W, cin, cout, np, relu;
+  const float *bias;
+  __nv_bfloat16 *y;
+  int y_cstride, y_coff;
+  float *yf;
+  const float *resid;
+  int *err;
+  int ty, tx;          // tiles along y and x
+  long long ntiles;
+  uint32_t wbytes;     // packed weights of all taps
+};
+
+__host__ __device__ constexpr size_t halo_smem_bytes(int cin, uint32_t wbytes) {
+  return (size_t)wbytes + 2 * (size_t)(cin / 8) * kHaloGS + 64 + 128;
+}
+
+__global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_constant__ CUtensorMap tmx,
+                                                              const __nv_bfloat16 *__restrict__ wp,
+                                                              const HaloArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  const int ngc = a.cin / 8;                       // channel groups
+  unsigned char *wsm = sm;                         // packed weights
+  unsigned char *halo = sm + a.wbytes;             // two halo buffers
+  const uint32_t hbytes = (uint32_t)ngc * kHaloGS;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(halo + 2 * hbytes);
+  // bar[0]: weights, bar[1..2]: halo buffers, bar[3]: MMAs of the tile
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t ncols = a.np <= 32 ? 32 : (a.np <= 64 ? 64 : 128);
+  if ((long long)blockIdx.x >= a.ntiles) return;   // uniform, before any allocation
+
+  if (warp == 0) {
+    tc::tmem_alloc(smem_u32(tslot), ncols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 4; i++) mbar_init(smem_u32(&bar[i]), 1);
+    mbar_fence_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(kTM, a.np, false, false);
+  const int ngn = a.np / 8;
+
+  auto tile_pos = [&](long long tile, int &n, int &z, int &y0, int &x0) {
+    const int bx = (int)(tile % a.tx);
+    long long r = tile / a.tx;
+    const int by = (int)(r % a.ty);
+    r /= a.ty;
+    z = (int)(r % a.D);
+    n = (int)(r / a.D);
+    y0 = by * kTileY;
+    x0 = bx * kTileX;
+  };
+  auto issue_halo = [&](long long tile, int buf) {
+    int n, z, y0, x0;
+    tile_pos(tile, n, z, y0, x0);
+    const uint32_t hb = smem_u32(&bar[1 + buf]);
+    mbar_arrive_expect_tx(hb, (uint32_t)ngc * (kHaloX * kHaloY * kHaloZ * 16));   // bytes the boxes carry
+    const uint32_t dst = smem_u32(halo + buf * hbytes);
+    for (int g = 0; g < ngc; g++)
+      tma_load_5d(dst + g * kHaloGS, &tmx, 8 * g, x0 - 1, y0 - 1, z - 1, n, hb);
+  };
+
+  if (tid == 0) {
+    prefetch_tmap(&tmx);
+    mbar_arrive_expect_tx(smem_u32(&bar[0]), a.wbytes);
+    bulk_load(smem_u32(wsm), wp, a.wbytes, smem_u32(&bar[0]));
+    issue_halo(blockIdx.x, 0);
+  }
+  bool ok = true;
+  int k = 0;               // tiles done by this CTA
+  int halo_issued = 1, halo_used = 0;
+  for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, k++) {
+    const int buf = k & 1;
+    if (tid == 0) {
+      const long long next = tile + gridDim.x;
+      if (ok && next < a.ntiles) {   // the other buffer's MMAs finished with the previous tile
+        issue_halo(next, buf ^ 1);
+        halo_issued++;
+      }
+      if (ok && k == 0) ok = mbar_wait_bounded(smem_u32(&bar[0]), 0, a.err, kErrFullWait);
+      if (ok) ok = mbar_wait_bounded(smem_u32(&bar[1 + buf]), (k >> 1) & 1, a.err, kErrFullWait);
+      if (ok) {
+        halo_used++;
+        tc::fence_after_sync();
+        const uint32_t h0 = smem_u32(halo + buf * hbytes), w0 = smem_u32(wsm);
+        bool first = true;
+        for (int t = 0; t < 27; t++) {
+          const int q = (t * 57) >> 9, r = t - 9 * q, q3 = (r * 11) >> 5;   // t = 9 dz' + 3 dy' + dx'
+          const uint32_t tap_off = (uint32_t)(((q * kHaloY + q3) * kHaloX + (r - 3 * q3)) * 16);
+          for (int s = 0; s < ngc / 2; s++) {
+            const uint64_t ad = tc::smem_desc(h0 + 2 * s * kHaloGS + tap_off, kHaloGS, kHaloX * 16);
+            const uint64_t bd =
+                tc::smem_desc(w0 + (uint32_t)((t * ngc + 2 * s) * ngn * 128), ngn * 128, 128);
+            tc::mma_bf16(tmem, ad, bd, idesc, first ? 0u : 1u);
+            first = false;
+          }
+        }
+        tc::mma_commit(smem_u32(&bar[3]));
+      }
+    }
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    if (!mbar_wait_bounded(smem_u32(&bar[3]), k & 1, a.err, kErrMmaWait)) ok = false;
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    tc::fence_after_sync();
+    // epilogue: TMEM lane = tile row r = 8 * (y - y0) + (x - x0)
+    int n, z, y0, x0;
+    tile_pos(tile, n, z, y0, x0);
+    const int r = warp * 32 + lane;
+    const int yy = y0 + (r >> 3), xx = x0 + (r & 7);
+    const bool vin = yy < a.H && xx < a.W;
+    const long long v = (((long long)n * a.D + z) * a.H + yy) * a.W + xx;
+    for (int n0 = 0; n0 < a.np; n0 += 16) {
+      float acc[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + n0, acc);
+      if (vin) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const int c = n0 + i;
+          float o = acc[i] + ((c < a.cout && a.bias) ? a.bias[c] : 0.f);
+          if (a.relu) o = fmaxf(o, 0.f);
+          acc[i] = o;
+        }
+        if (a.y) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 8) {
+            if (n0 + i + 8 <= a.cout) {
+              __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+              for (int e = 0; e < 8; e++) h[e] = __float2bfloat16_rn(acc[i + e]);
+              *reinterpret_cast<uint4 *>(a.y + v * a.y_cstride + a.y_coff + n0 + i) =
+                  *reinterpret_cast<const uint4 *>(h);
+            }
+          }
+        }
+        if (a.yf) {
+#pragma unroll
+          for (int i = 0; i < 16; i++)
+            if (n0 + i < a.cout)
+              a.yf[v * a.cout + n0 + i] = acc[i] + (a.resid ? a.resid[v * a.cout + n0 + i] : 0.f);
+        }
+      }
+    }
+    // the accumulator is read: the next tile's MMAs may overwrite it
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  // never leave with a copy in flight (an error path may have skipped waits)
+  if (tid == 0) {
+    if (halo_used == 0 && halo_issued > 0) mbar_wait_bounded(smem_u32(&bar[0]), 0, a.err, kErrDrainWait);
+    for (int i = halo_used; i < halo_issued; i++)
+      mbar_wait_bounded(smem_u32(&bar[1 + (i & 1)]), (i >> 1) & 1, a.err, kErrDrainWait);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -653,9 +842,90 @@ int check_conv_args(int cin, int cstride, int coff, int cout, int ntap) {
   return 0;
 }
 int np_of(int cout) { return ((cout + 15) / 16) * 16; }
+
+// The halo-staged convolution takes 3x3x3 layers whose input channels are a
+// multiple of 16, whose planes hold at least one 16 x 8 tile and whose
+// weights and two halo buffers fit in 200 KB of shared memory (one CTA per SM
+// for the largest of them).
+constexpr size_t kHaloMaxSmem = 200 * 1024;
+bool g_halo_enabled = true;
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+int g_num_sms = 0;
+
+int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
+              const void *wpacked, uint32_t wbytes, const float *bias, int cout, int np, int relu,
+              void *y, int y_cstride, int y_coff, float *yf, const float *resid, int *err,
+              cudaStream_t st) {
+  if (!g_encode) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        !fn || q != cudaDriverEntryPointSuccess)
+      return set_error("unet conv: cuTensorMapEncodeTiled is unavailable");
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return set_error("unet conv: cannot query the device");
+  }
+  // x as a 5-D tensor (channels of the view, W, H, D, volumes), channels innermost
+  const __nv_bfloat16 *base = (const __nv_bfloat16 *)x + x_coff;
+  if (reinterpret_cast<uintptr_t>(base) % 16) return set_error("unet conv: input view not 16-byte aligned");
+  const cuuint64_t cs = (cuuint64_t)x_cstride * 2;
+  cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)nb};
+  cuuint64_t strides[4] = {cs, cs * W, cs * W * H, cs * W * H * D};
+  cuuint32_t box[5] = {8, (cuuint32_t)kHaloX, (cuuint32_t)kHaloY, (cuuint32_t)kHaloZ, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUtensorMap tm;
+  CUresult r = g_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(base), dims,
+                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error("unet conv: cuTensorMapEncodeTiled failed (%d)", (int)r);
+  HaloArgs a;
+  a.nb = nb; a.D = D; a.H = H; a.W = W; a.cin = cin; a.cout = cout; a.np = np; a.relu = relu;
+  a.bias = bias; a.y = (__nv_bfloat16 *)y; a.y_cstride = y_cstride; a.y_coff = y_coff;
+  a.yf = yf; a.resid = resid; a.err = err;
+  a.ty = (H + kTileY - 1) / kTileY;
+  a.tx = (W + kTileX - 1) / kTileX;
+  a.ntiles = (long long)nb * D * a.ty * a.tx;
+  a.wbytes = wbytes;
+  const size_t smem = halo_smem_bytes(cin, wbytes);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(conv_halo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kHaloMaxSmem);
+    // the persistent grid is sized from the occupancy query: ask for the
+    // full shared-memory carve-out so that every CTA of the grid is resident
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(conv_halo_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return set_error("unet conv: %s", cudaGetErrorString(e));
+    attr = true;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_halo_kernel, kUThreads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    return set_error("unet conv: the halo kernel does not fit an SM");
+  // tensor memory: at most 512 columns per SM across resident CTAs
+  const int ncols = np <= 32 ? 32 : (np <= 64 ? 64 : 128);
+  if (per_sm * ncols > 512) per_sm = 512 / ncols;
+  long long grid = (long long)g_num_sms * per_sm;
+  if (grid > a.ntiles) grid = a.ntiles;
+  conv_halo_kernel<<<(unsigned)grid, kUThreads, smem, st>>>(tm, (const __nv_bfloat16 *)wpacked, a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
+}
 }  // namespace
 
 extern "C" {
+
+int sepx_unet_set_halo(int enable) {
+  const int prev = g_halo_enabled ? 1 : 0;
+  g_halo_enabled = enable != 0;
+  return prev;
+}
 
 int sepx_unet_packed_elems(int cout, int cin_p, int ntap, int transpose) {
   const int nout = transpose ? cin_p : cout, kin = transpose ? ((cout + 7) / 8) * 8 : cin_p;
@@ -690,6 +960,13 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
   const long long V = (long long)nb * D * H * W;
   if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
     return set_error("unet conv: volume too large (%lld voxels)", V);
+  if (ntap == 27 && cin % 16 == 0 && H >= kTileY && W >= kTileX && g_halo_enabled) {
+    const uint32_t wbytes = (uint32_t)(27 * (cin / 8) * (np / 8) * 128);
+    const size_t hs = halo_smem_bytes(cin, wbytes);
+    if (hs <= kHaloMaxSmem) return conv_halo(x, x_cstride, x_coff, nb, D, H, W, cin, wpacked, wbytes,
+                                             bias, cout, np, relu, y, y_cstride, y_coff, yf, resid,
+                                             err, (cudaStream_t)stream);
+  }
   const size_t smem = conv_smem(np);
   static bool attr = false;
   if (!attr) {

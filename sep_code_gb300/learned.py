@@ -242,7 +242,11 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
             "image_rel_l2_vs_plain_cg": rel(m_nn, m_plain),
             "image_rel_l2_vs_true": rel(m_nn, s.refl),
         }
-    first = by_policy[policies[0]]
+    first = by_policy[policies[0]] if policies else None
+
+    def pick(key):
+        return first[key] if first else None
+
     return {
         "workload": s.name, "iterations": niter, "target": target or None,
         "store": f"{snap_prec} every {snap_js} steps",
@@ -250,11 +254,11 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
         "plain": {"rel_residual": rp.tolist(), "seconds": s_plain.tolist()},
         "learned": first,
         "learned_by_policy": by_policy,
-        "time_to_1e-2": {"plain": t_to(rp, s_plain, 1e-2), "learned": first["time_to_1e-2"]},
+        "time_to_1e-2": {"plain": t_to(rp, s_plain, 1e-2), "learned": pick("time_to_1e-2")},
         "time_to_plain_final_residual": {"plain": float(s_plain[-1]),
-                                         "learned": first["time_to_plain_final_residual"]},
-        "image_rel_l2_vs_plain_cg": {"learned_final": first["image_rel_l2_vs_plain_cg"]},
-        "image_rel_l2_vs_true": {"plain": rel(m_plain, s.refl), "learned": first["image_rel_l2_vs_true"]},
+                                         "learned": pick("time_to_plain_final_residual")},
+        "image_rel_l2_vs_plain_cg": {"learned_final": pick("image_rel_l2_vs_plain_cg")},
+        "image_rel_l2_vs_true": {"plain": rel(m_plain, s.refl), "learned": pick("image_rel_l2_vs_true")},
     }
 
 
@@ -278,7 +282,8 @@ def main(argv=None):
     c.add_argument("--iters", type=int, default=20)
     c.add_argument("--weights", default=str(WEIGHTS))
     c.add_argument("--out", default=None)
-    c.add_argument("--policies", default="fallback", help="comma list of fallback,adaptive")
+    c.add_argument("--policies", default="fallback",
+                   help="comma list of fallback,adaptive (empty: plain CG only)")
     c.add_argument("--probe-every", type=int, default=8)
     c.add_argument("--target", type=float, default=0.0)
     a = p.parse_args(argv)
@@ -296,7 +301,7 @@ def main(argv=None):
     else:
         s = lsrtm_survey(a.n, a.nt, a.shots)
         res = lsrtm_compare(s, a.iters, net=load_network(a.weights), verbose=True,
-                            policies=tuple(a.policies.split(",")), probe_every=a.probe_every,
+                            policies=tuple(x for x in a.policies.split(",") if x), probe_every=a.probe_every,
                             target=a.target)
         txt = json.dumps(res)
         print(txt)

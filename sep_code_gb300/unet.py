@@ -50,6 +50,7 @@ _SIGS = {
     "sepx_unet_mse": [_vp, _vp, _ll, _vp, _i, _vp, _vp],
     "sepx_unet_adam": [_vp, _vp, _vp, _vp, _ll, _f, _f, _f, _f, _i, _vp],
     "sepx_unet_status": [],
+    "sepx_unet_set_halo": [_i],
 }
 for _n, _a in _SIGS.items():
     getattr(lib, _n).argtypes = _a

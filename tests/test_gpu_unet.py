@@ -208,3 +208,88 @@ def test_training_reduces_loss(net):
     losses = [model.train_step(xt, tt, lr=2e-3) for _ in range(60)]
     assert model.status() == 0
     assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
+
+
+HALO_CASES = [(2, 8, 24, 20, 16, 16, 0), (1, 6, 32, 16, 32, 48, 0), (1, 5, 16, 8, 48, 16, 1),
+              (1, 4, 17, 9, 16, 32, 1), (2, 3, 16, 24, 32, 32, 0)]
+
+
+@pytest.mark.parametrize("nb,D,H,W,cin,cout,tr", HALO_CASES)
+def test_halo_conv_matches_gather_and_oracle(net, nb, D, H, W, cin, cout, tr):
+    """the halo-staged kernel (input halo by TMA, taps as shifted shared-memory
+    descriptors) against the per-tap gather kernel and the FP64 restatement:
+    partial tiles (H % 16, W % 8), several volumes, forward and data-gradient
+    packings"""
+    from sep_code_gb300._lib import lib
+    rng = np.random.default_rng(nb * 1000 + D * 100 + H + cin)
+    lib.sepx_setup_cuda(1)
+    st = lib.sepx_get_stream()
+    # forward operand (tr 0): w [27][cin][cout]; data-gradient operand (tr 1):
+    # the layer cout -> cin, so its master weights are [27][cout][cin]
+    w = (rng.standard_normal((27, cout if tr else cin, cin if tr else cout)) / np.sqrt(27 * cin)).astype(np.float32)
+    x = U.bf16(rng.standard_normal((nb, D, H, W, cin)))
+    wt = torch.tensor(w).cuda()
+    lay_out, lay_in = (cin, cout) if tr else (cout, cin)
+    pk = torch.zeros(net.lib.sepx_unet_packed_elems(lay_out, lay_in, 27, tr), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_pack_weights(net._p(wt), lay_out, lay_in, 27, tr, net._p(pk), st))
+    xt = _bf(x)
+    V = nb * D * H * W
+    outs = []
+    for halo in (1, 0):
+        prev = lib.sepx_unet_set_halo(halo)
+        yf = torch.zeros(V * cout, dtype=torch.float32).cuda()
+        torch.cuda.synchronize()
+        net._chk(net.lib.sepx_unet_conv_fwd(net._p(xt), cin, 0, nb, D, H, W, cin, 27, net._p(pk), None, cout,
+                                            0, None, 0, 0, net._p(yf), None, st))
+        _sync(net)
+        lib.sepx_unet_set_halo(prev)
+        outs.append(yf.cpu().numpy())
+    assert net.lib.sepx_unet_status() == 0
+    if tr:
+        want = U.conv_dgrad(x, U.bf16(w))
+    else:
+        want = U.conv_fwd(x, U.bf16(w), None, False)
+    assert rel_l2(outs[0].reshape(want.shape), want) <= 1e-5, rel_l2(outs[0].reshape(want.shape), want)
+    assert rel_l2(outs[0], outs[1]) <= 1e-6
+
+
+def test_halo_conv_speed_384(net):
+    """16 -> 16 channels on a 384^3 volume, both kernels, CUDA events on the
+    library stream; prints UNET_HALO {json}"""
+    import json
+    from sep_code_gb300._lib import lib
+    lib.sepx_setup_cuda(1)
+    st = lib.sepx_get_stream()
+    stream = torch.cuda.ExternalStream(st)
+    D = H = W = 384
+    res = {}
+    for cin, cout in ((16, 16), (32, 32), (48, 16)):
+        g = torch.Generator(device="cuda").manual_seed(cin)
+        x = torch.randn(D * H * W * cin, device="cuda", generator=g).to(torch.bfloat16)
+        wt = torch.randn(27 * cin * cout, device="cuda", generator=g) * 0.05
+        pk = torch.zeros(net.lib.sepx_unet_packed_elems(cout, cin, 27, 0), dtype=torch.bfloat16).cuda()
+        y = torch.empty(D * H * W * cout, dtype=torch.bfloat16, device="cuda")
+        torch.cuda.synchronize()
+        net._chk(net.lib.sepx_unet_pack_weights(net._p(wt), cout, cin, 27, 0, net._p(pk), st))
+        flops = 2.0 * D * H * W * 27 * cin * cout
+        for halo in (1, 0):
+            prev = lib.sepx_unet_set_halo(halo)
+
+            def run():
+                net._chk(net.lib.sepx_unet_conv_fwd(net._p(x), cin, 0, 1, D, H, W, cin, 27, net._p(pk), None,
+                                                    cout, 1, net._p(y), cout, 0, None, None, st))
+            run()
+            stream.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(3):
+                run()
+            b.record(stream)
+            b.synchronize()
+            lib.sepx_unet_set_halo(prev)
+            ms = a.elapsed_time(b) / 3
+            res[f"{cin}->{cout} {'halo' if halo else 'gather'}"] = {"ms": ms, "TFLOP_s": flops / ms / 1e9}
+        del x, y
+    assert net.lib.sepx_unet_status() == 0
+    print("UNET_HALO " + json.dumps(res))
