@@ -285,10 +285,15 @@ struct HaloArgs {
   int ty, tx;          // tiles along y and x
   long long ntiles;
   uint32_t wbytes;     // packed weights of all taps
+  int nbuf;            // halo buffers: 2 (prefetch during the MMAs) or 1
 };
 
-__host__ __device__ constexpr size_t halo_smem_bytes(int cin, uint32_t wbytes) {
-  return (size_t)wbytes + 2 * (size_t)(cin / 8) * kHaloGS + 64 + 128;
+// channel groups held per halo buffer: cin/8 rounded up to even (an odd
+// count gets one all-zero group, the channel box lying wholly outside x)
+__host__ __device__ constexpr int halo_groups(int cin) { return ((cin / 8) + 1) & ~1; }
+
+__host__ __device__ constexpr size_t halo_smem_bytes(int cin, uint32_t wbytes, int nbuf) {
+  return (size_t)wbytes + (size_t)nbuf * (size_t)halo_groups(cin) * kHaloGS + 64 + 128;
 }
 
 __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_constant__ CUtensorMap tmx,
@@ -297,11 +302,12 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
-  const int ngc = a.cin / 8;                       // channel groups
+  const int ngc = a.cin / 8;                       // channel groups of x
+  const int ngh = halo_groups(a.cin);              // groups held (even)
   unsigned char *wsm = sm;                         // packed weights
-  unsigned char *halo = sm + a.wbytes;             // two halo buffers
-  const uint32_t hbytes = (uint32_t)ngc * kHaloGS;
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(halo + 2 * hbytes);
+  unsigned char *halo = sm + a.wbytes;             // a.nbuf halo buffers
+  const uint32_t hbytes = (uint32_t)ngh * kHaloGS;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(halo + a.nbuf * hbytes);
   // bar[0]: weights, bar[1..2]: halo buffers, bar[3]: MMAs of the tile
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -337,9 +343,9 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
     int n, z, y0, x0;
     tile_pos(tile, n, z, y0, x0);
     const uint32_t hb = smem_u32(&bar[1 + buf]);
-    mbar_arrive_expect_tx(hb, (uint32_t)ngc * (kHaloX * kHaloY * kHaloZ * 16));   // bytes the boxes carry
+    mbar_arrive_expect_tx(hb, (uint32_t)ngh * (kHaloX * kHaloY * kHaloZ * 16));   // bytes the boxes carry
     const uint32_t dst = smem_u32(halo + buf * hbytes);
-    for (int g = 0; g < ngc; g++)
+    for (int g = 0; g < ngh; g++)
       tma_load_5d(dst + g * kHaloGS, &tmx, 8 * g, x0 - 1, y0 - 1, z - 1, n, hb);
   };
 
@@ -349,19 +355,23 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
     bulk_load(smem_u32(wsm), wp, a.wbytes, smem_u32(&bar[0]));
     issue_halo(blockIdx.x, 0);
   }
+  // halo copy i (of this CTA) lands in buffer buf_of(i) and completes phase
+  // par_of(i) of that buffer's barrier
+  auto buf_of = [&](int i) { return a.nbuf == 2 ? (i & 1) : 0; };
+  auto par_of = [&](int i) { return (uint32_t)((a.nbuf == 2 ? (i >> 1) : i) & 1); };
   bool ok = true;
   int k = 0;               // tiles done by this CTA
   int halo_issued = 1, halo_used = 0;
   for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, k++) {
-    const int buf = k & 1;
+    const int buf = buf_of(k);
+    const long long next = tile + gridDim.x;
     if (tid == 0) {
-      const long long next = tile + gridDim.x;
-      if (ok && next < a.ntiles) {   // the other buffer's MMAs finished with the previous tile
-        issue_halo(next, buf ^ 1);
+      if (ok && a.nbuf == 2 && next < a.ntiles) {   // the other buffer's MMAs finished with the previous tile
+        issue_halo(next, buf_of(k + 1));
         halo_issued++;
       }
       if (ok && k == 0) ok = mbar_wait_bounded(smem_u32(&bar[0]), 0, a.err, kErrFullWait);
-      if (ok) ok = mbar_wait_bounded(smem_u32(&bar[1 + buf]), (k >> 1) & 1, a.err, kErrFullWait);
+      if (ok) ok = mbar_wait_bounded(smem_u32(&bar[1 + buf]), par_of(k), a.err, kErrFullWait);
       if (ok) {
         halo_used++;
         tc::fence_after_sync();
@@ -370,7 +380,11 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
         for (int t = 0; t < 27; t++) {
           const int q = (t * 57) >> 9, r = t - 9 * q, q3 = (r * 11) >> 5;   // t = 9 dz' + 3 dy' + dx'
           const uint32_t tap_off = (uint32_t)(((q * kHaloY + q3) * kHaloX + (r - 3 * q3)) * 16);
-          for (int s = 0; s < ngc / 2; s++) {
+          // K16 step s: channel groups 2s, 2s + 1; for odd ngc the last step
+          // pairs group ngc - 1 with the zero group, whose B partner (the
+          // next tap's first group, or the zero padding after the last tap)
+          // then multiplies zeros
+          for (int s = 0; s < ngh / 2; s++) {
             const uint64_t ad = tc::smem_desc(h0 + 2 * s * kHaloGS + tap_off, kHaloGS, kHaloX * 16);
             const uint64_t bd =
                 tc::smem_desc(w0 + (uint32_t)((t * ngc + 2 * s) * ngn * 128), ngn * 128, 128);
@@ -387,6 +401,10 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
     ok = __syncthreads_and(ok);
     if (!ok) break;
     tc::fence_after_sync();
+    if (tid == 0 && a.nbuf == 1 && next < a.ntiles) {   // the MMAs are done with the only buffer
+      issue_halo(next, 0);
+      halo_issued++;
+    }
     // epilogue: TMEM lane = tile row r = 8 * (y - y0) + (x - x0)
     int n, z, y0, x0;
     tile_pos(tile, n, z, y0, x0);
@@ -433,7 +451,7 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
   if (tid == 0) {
     if (halo_used == 0 && halo_issued > 0) mbar_wait_bounded(smem_u32(&bar[0]), 0, a.err, kErrDrainWait);
     for (int i = halo_used; i < halo_issued; i++)
-      mbar_wait_bounded(smem_u32(&bar[1 + (i & 1)]), (i >> 1) & 1, a.err, kErrDrainWait);
+      mbar_wait_bounded(smem_u32(&bar[1 + buf_of(i)]), par_of(i), a.err, kErrDrainWait);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -843,14 +861,14 @@ int check_conv_args(int cin, int cstride, int coff, int cout, int ntap) {
 }
 int np_of(int cout) { return ((cout + 15) / 16) * 16; }
 
-// The halo-staged convolution takes 3x3x3 layers whose input channels are a
-// multiple of 16, whose planes hold at least one 16 x 8 tile and whose
-// weights and two halo buffers fit in 200 KB of shared memory (one CTA per SM
-// for the largest of them).
+// The halo-staged convolution takes 3x3x3 layers whose planes hold at least
+// one 16 x 8 tile and whose weights and a halo buffer fit in 200 KB of shared
+// memory (one CTA per SM for the largest of them).
 constexpr size_t kHaloMaxSmem = 200 * 1024;
 bool g_halo_enabled = true;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
+size_t g_smem_per_sm = 0, g_smem_reserved = 0;
 
 int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
               const void *wpacked, uint32_t wbytes, const float *bias, int cout, int np, int relu,
@@ -864,10 +882,14 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
         !fn || q != cudaDriverEntryPointSuccess)
       return set_error("unet conv: cuTensorMapEncodeTiled is unavailable");
     g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    int dev = 0;
+    int dev = 0, smem_sm = 0, resv = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
       return set_error("unet conv: cannot query the device");
+    g_smem_per_sm = (size_t)smem_sm;
+    g_smem_reserved = (size_t)resv;
   }
   // x as a 5-D tensor (channels of the view, W, H, D, volumes), channels innermost
   const __nv_bfloat16 *base = (const __nv_bfloat16 *)x + x_coff;
@@ -890,7 +912,19 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
   a.tx = (W + kTileX - 1) / kTileX;
   a.ntiles = (long long)nb * D * a.ty * a.tx;
   a.wbytes = wbytes;
-  const size_t smem = halo_smem_bytes(cin, wbytes);
+  // resident CTAs per SM from the shared memory each needs (the CTAs of the
+  // persistent grid must all be resident): two halo buffers unless one
+  // buffer fits two CTAs per SM where two buffers fit only one
+  auto fit = [&](int nbuf) {
+    const size_t per = ((halo_smem_bytes(cin, wbytes, nbuf) + 127) / 128) * 128 + g_smem_reserved;
+    return (int)(g_smem_per_sm / per);
+  };
+  const bool two_fit = halo_smem_bytes(cin, wbytes, 2) <= kHaloMaxSmem;
+  a.nbuf = (two_fit && (fit(2) >= 2 || fit(1) < 2)) ? 2 : 1;
+  int per_sm = fit(a.nbuf);
+  if (per_sm < 1) return set_error("unet conv: the halo kernel does not fit an SM");
+  if (per_sm > 8) per_sm = 8;
+  const size_t smem = halo_smem_bytes(cin, wbytes, a.nbuf);
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(conv_halo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -903,11 +937,6 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
     if (e != cudaSuccess) return set_error("unet conv: %s", cudaGetErrorString(e));
     attr = true;
   }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_halo_kernel, kUThreads, smem) !=
-          cudaSuccess ||
-      per_sm < 1)
-    return set_error("unet conv: the halo kernel does not fit an SM");
   // tensor memory: at most 512 columns per SM across resident CTAs
   const int ncols = np <= 32 ? 32 : (np <= 64 ? 64 : 128);
   if (per_sm * ncols > 512) per_sm = 512 / ncols;
@@ -960,12 +989,15 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
   const long long V = (long long)nb * D * H * W;
   if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
     return set_error("unet conv: volume too large (%lld voxels)", V);
-  if (ntap == 27 && cin % 16 == 0 && H >= kTileY && W >= kTileX && g_halo_enabled) {
-    const uint32_t wbytes = (uint32_t)(27 * (cin / 8) * (np / 8) * 128);
-    const size_t hs = halo_smem_bytes(cin, wbytes);
-    if (hs <= kHaloMaxSmem) return conv_halo(x, x_cstride, x_coff, nb, D, H, W, cin, wpacked, wbytes,
-                                             bias, cout, np, relu, y, y_cstride, y_coff, yf, resid,
-                                             err, (cudaStream_t)stream);
+  if (ntap == 27 && H >= kTileY && W >= kTileX && g_halo_enabled) {
+    // packed weights of the 27 taps, plus one K group for an odd group count
+    // (the packing pads with zeros up to a multiple of 8 groups, and 27 * an
+    // odd count is never one)
+    const int ngc = cin / 8;
+    const uint32_t wbytes = (uint32_t)((27 * ngc + (ngc & 1)) * (np / 8) * 128);
+    if (halo_smem_bytes(cin, wbytes, 1) <= kHaloMaxSmem)
+      return conv_halo(x, x_cstride, x_coff, nb, D, H, W, cin, wpacked, wbytes, bias, cout, np, relu, y,
+                       y_cstride, y_coff, yf, resid, err, (cudaStream_t)stream);
   }
   const size_t smem = conv_smem(np);
   static bool attr = false;

@@ -211,7 +211,9 @@ def test_training_reduces_loss(net):
 
 
 HALO_CASES = [(2, 8, 24, 20, 16, 16, 0), (1, 6, 32, 16, 32, 48, 0), (1, 5, 16, 8, 48, 16, 1),
-              (1, 4, 17, 9, 16, 32, 1), (2, 3, 16, 24, 32, 32, 0)]
+              (1, 4, 17, 9, 16, 32, 1), (2, 3, 16, 24, 32, 32, 0),
+              # odd channel-group counts (one zero group in the halo)
+              (2, 4, 16, 8, 8, 16, 0), (1, 3, 20, 12, 24, 16, 0), (1, 3, 16, 16, 24, 32, 1)]
 
 
 @pytest.mark.parametrize("nb,D,H,W,cin,cout,tr", HALO_CASES)
@@ -219,7 +221,7 @@ def test_halo_conv_matches_gather_and_oracle(net, nb, D, H, W, cin, cout, tr):
     """the halo-staged kernel (input halo by TMA, taps as shifted shared-memory
     descriptors) against the per-tap gather kernel and the FP64 restatement:
     partial tiles (H % 16, W % 8), several volumes, forward and data-gradient
-    packings"""
+    packings, even and odd numbers of 8-channel groups"""
     from sep_code_gb300._lib import lib
     rng = np.random.default_rng(nb * 1000 + D * 100 + H + cin)
     lib.sepx_setup_cuda(1)
@@ -264,7 +266,7 @@ def test_halo_conv_speed_384(net):
     stream = torch.cuda.ExternalStream(st)
     D = H = W = 384
     res = {}
-    for cin, cout in ((16, 16), (32, 32), (48, 16)):
+    for cin, cout in ((8, 16), (16, 16), (32, 32), (48, 16)):
         g = torch.Generator(device="cuda").manual_seed(cin)
         x = torch.randn(D * H * W * cin, device="cuda", generator=g).to(torch.bfloat16)
         wt = torch.randn(27 * cin * cout, device="cuda", generator=g) * 0.05
@@ -293,3 +295,51 @@ def test_halo_conv_speed_384(net):
         del x, y
     assert net.lib.sepx_unet_status() == 0
     print("UNET_HALO " + json.dumps(res))
+
+
+def test_network_speed(net):
+    """whole-network timing, halo-staged and gather convolutions: one Adam
+    training step on a batch of 4 x 64^3 and the inference of one 384^3
+    search direction; CUDA events on the library stream; prints UNET_NET
+    {json} with the convolution FLOPs per second"""
+    import json
+    from sep_code_gb300._lib import lib
+    model = net.UNet3D(seed=3)
+    stream = model.stream
+    g = torch.Generator(device="cuda").manual_seed(9)
+
+    def conv_flops(nb, n):
+        f = 0.0
+        lvl = {"e1": 0, "e2": 1, "e3": 2, "b4": 3, "d3": 2, "d2": 1, "d1": 0, "ou": 0}
+        for L in net.LAYERS:
+            v = nb * (n >> lvl[L.name[:2]]) ** 3
+            f += 2.0 * v * L.ntap * L.cin * L.cout
+        return f
+
+    def timed(fn, reps):
+        fn()
+        stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    x = torch.randn(4, 64, 64, 64, device="cuda", generator=g)
+    t = torch.randn(4, 64, 64, 64, device="cuda", generator=g)
+    big = torch.randn(1, 384, 384, 384, device="cuda", generator=g)
+    torch.cuda.synchronize()
+    res = {}
+    for halo in (1, 0):
+        prev = lib.sepx_unet_set_halo(halo)
+        tag = "halo" if halo else "gather"
+        ms = timed(lambda: model.train_step(x, t, lr=1e-4), 5)
+        # forward + data gradient + weight gradient = 3 x the forward FLOPs
+        res[f"train_step_4x64^3 {tag}"] = {"ms": ms, "TFLOP_s": 3 * conv_flops(4, 64) / ms / 1e9}
+        ms = timed(lambda: model.forward_device(big), 2)
+        res[f"inference_384^3 {tag}"] = {"ms": ms, "TFLOP_s": conv_flops(1, 384) / ms / 1e9}
+        lib.sepx_unet_set_halo(prev)
+    assert model.status() == 0
+    print("UNET_NET " + json.dumps(res))
