@@ -392,3 +392,56 @@ class UNet3D:
 
     def status(self) -> int:
         return lib.sepx_unet_status()
+
+
+def conv_layer_timing(cin: int, cout: int, nb: int = 4, n: int = 64, reps: int = 2, halo: bool = True,
+                      seed: int = 0) -> float:
+    """run one 3x3x3 convolution (random BF16 input and weights, ReLU, BF16
+    out) on nb volumes of n^3 voxels `reps` times; returns milliseconds per run
+    (CUDA events on the library stream)"""
+    import torch
+    lib.sepx_setup_cuda(1)
+    st = lib.sepx_get_stream()
+    stream = torch.cuda.ExternalStream(st)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    V = nb * n ** 3
+    x = torch.randn(V * cin, device="cuda", generator=g).to(torch.bfloat16)
+    w = torch.randn(27 * cin * cout, device="cuda", generator=g) * 0.05
+    pk = torch.zeros(lib.sepx_unet_packed_elems(cout, cin, 27, 0), dtype=torch.bfloat16, device="cuda")
+    y = torch.empty(V * cout, dtype=torch.bfloat16, device="cuda")
+    torch.cuda.synchronize()
+    _chk(lib.sepx_unet_pack_weights(_p(w), cout, cin, 27, 0, _p(pk), st))
+    prev = lib.sepx_unet_set_halo(1 if halo else 0)
+    try:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            _chk(lib.sepx_unet_conv_fwd(_p(x), cin, 0, nb, n, n, n, cin, 27, _p(pk), None, cout, 1, _p(y),
+                                        cout, 0, None, None, st))
+        b.record(stream)
+        b.synchronize()
+    finally:
+        lib.sepx_unet_set_halo(prev)
+    if lib.sepx_unet_status() != 0:
+        raise SepxError("convolution kernel reported a device error")
+    return a.elapsed_time(b) / reps
+
+
+def main(argv=None):
+    import argparse
+    p = argparse.ArgumentParser(description="time single U-Net convolution layers")
+    p.add_argument("--layers", default="16:16,48:16", help="comma list of cin:cout")
+    p.add_argument("--nb", type=int, default=4)
+    p.add_argument("--n", type=int, default=64)
+    p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--gather", action="store_true", help="use the per-tap gather kernel")
+    a = p.parse_args(argv)
+    for spec in a.layers.split(","):
+        cin, cout = (int(v) for v in spec.split(":"))
+        ms = conv_layer_timing(cin, cout, a.nb, a.n, a.reps, halo=not a.gather)
+        flops = 2.0 * a.nb * a.n ** 3 * 27 * cin * cout
+        print(f"conv {cin}->{cout} on {a.nb} x {a.n}^3: {ms:.3f} ms, {flops / ms / 1e9:.1f} TFLOP/s")
+
+
+if __name__ == "__main__":
+    main()
