@@ -35,7 +35,7 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
                        int ntap, const void *wpacked, const float *bias, int cout, int relu, void *y,
                        int y_cstride, int y_coff, float *yf, const float *resid, void *stream);
 /* 3x3x3 layers whose planes are at least 16 x 8 voxels and whose packed
- * weights and input halo fit in 200 KB of shared memory run on the
+ * weights and input halo fit in 227 KB of shared memory run on the
  * halo-staged kernel; enable = 0 sends every layer to the per-tap gather
  * kernel.  Returns the previous setting. */
 int sepx_unet_set_halo(int enable);

@@ -293,12 +293,21 @@ struct HaloArgs {
 __host__ __device__ constexpr int halo_groups(int cin) { return ((cin / 8) + 1) & ~1; }
 
 __host__ __device__ constexpr size_t halo_smem_bytes(int cin, uint32_t wbytes, int nbuf) {
-  return (size_t)wbytes + (size_t)nbuf * (size_t)halo_groups(cin) * kHaloGS + 64 + 128;
+  return (size_t)wbytes + (size_t)nbuf * (size_t)halo_groups(cin) * kHaloGS + 128 + 128;
 }
 
-__global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_constant__ CUtensorMap tmx,
-                                                              const __nv_bfloat16 *__restrict__ wp,
-                                                              const HaloArgs a) {
+// Warp roles: warp 4 (lane 0) loads the weights and the halos and issues the
+// MMAs; warps 0-3 run the epilogue (warp w owns tensor-memory lanes
+// 32w..32w+31 = tile rows).  Two accumulators in tensor memory: the MMAs of
+// tile k+1 run while the epilogue of tile k reads the other one.
+// Barriers: full[b] halo buffer b loaded (TMA), hfree[b] the MMAs reading
+// halo buffer b are done (tcgen05.commit), acc[a] accumulator a complete
+// (commit), afree[a] accumulator a read by the 4 epilogue warps, wbar weights.
+constexpr int kHaloThreads = 160;
+
+__global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_constant__ CUtensorMap tmx,
+                                                                 const __nv_bfloat16 *__restrict__ wp,
+                                                                 const HaloArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -308,28 +317,37 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
   unsigned char *halo = sm + a.wbytes;             // a.nbuf halo buffers
   const uint32_t hbytes = (uint32_t)ngh * kHaloGS;
   unsigned long long *bar = reinterpret_cast<unsigned long long *>(halo + a.nbuf * hbytes);
-  // bar[0]: weights, bar[1..2]: halo buffers, bar[3]: MMAs of the tile
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
+  unsigned long long *full = bar, *hfree = bar + 2, *accb = bar + 4, *afree = bar + 6, *wbar = bar + 8;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 9);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t ncols = a.np <= 32 ? 32 : (a.np <= 64 ? 64 : 128);
+  const uint32_t acols = a.np <= 32 ? 32 : (a.np <= 64 ? 64 : 128);   // per accumulator
+  const uint32_t ncols = 2 * acols;
   if ((long long)blockIdx.x >= a.ntiles) return;   // uniform, before any allocation
+  const int ntile = (int)((a.ntiles - 1 - blockIdx.x) / gridDim.x) + 1;   // tiles of this CTA
 
   if (warp == 0) {
     tc::tmem_alloc(smem_u32(tslot), ncols);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int i = 0; i < 4; i++) mbar_init(smem_u32(&bar[i]), 1);
+    for (int i = 0; i < 2; i++) {
+      mbar_init(smem_u32(&full[i]), 1);
+      mbar_init(smem_u32(&hfree[i]), 1);
+      mbar_init(smem_u32(&accb[i]), 1);
+      mbar_init(smem_u32(&afree[i]), 4);
+    }
+    mbar_init(smem_u32(wbar), 1);
+    *abort_flag = 0;
     mbar_fence_init();
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = tc::idesc_bf16(kTM, a.np, false, false);
-  const int ngn = a.np / 8;
 
-  auto tile_pos = [&](long long tile, int &n, int &z, int &y0, int &x0) {
+  auto tile_pos = [&](int k, int &n, int &z, int &y0, int &x0) {
+    const long long tile = blockIdx.x + (long long)k * gridDim.x;
     const int bx = (int)(tile % a.tx);
     long long r = tile / a.tx;
     const int by = (int)(r % a.ty);
@@ -339,43 +357,44 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
     y0 = by * kTileY;
     x0 = bx * kTileX;
   };
-  auto issue_halo = [&](long long tile, int buf) {
-    int n, z, y0, x0;
-    tile_pos(tile, n, z, y0, x0);
-    const uint32_t hb = smem_u32(&bar[1 + buf]);
-    mbar_arrive_expect_tx(hb, (uint32_t)ngh * (kHaloX * kHaloY * kHaloZ * 16));   // bytes the boxes carry
-    const uint32_t dst = smem_u32(halo + buf * hbytes);
-    for (int g = 0; g < ngh; g++)
-      tma_load_5d(dst + g * kHaloGS, &tmx, 8 * g, x0 - 1, y0 - 1, z - 1, n, hb);
-  };
+  // halo copy k lands in buffer k % nbuf; its barrier phases alternate per use
+  auto hbuf = [&](int k) { return a.nbuf == 2 ? (k & 1) : 0; };
+  auto hpar = [&](int k) { return (uint32_t)((a.nbuf == 2 ? (k >> 1) : k) & 1); };
 
-  if (tid == 0) {
-    prefetch_tmap(&tmx);
-    mbar_arrive_expect_tx(smem_u32(&bar[0]), a.wbytes);
-    bulk_load(smem_u32(wsm), wp, a.wbytes, smem_u32(&bar[0]));
-    issue_halo(blockIdx.x, 0);
-  }
-  // halo copy i (of this CTA) lands in buffer buf_of(i) and completes phase
-  // par_of(i) of that buffer's barrier
-  auto buf_of = [&](int i) { return a.nbuf == 2 ? (i & 1) : 0; };
-  auto par_of = [&](int i) { return (uint32_t)((a.nbuf == 2 ? (i >> 1) : i) & 1); };
-  bool ok = true;
-  int k = 0;               // tiles done by this CTA
-  int halo_issued = 1, halo_used = 0;
-  for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, k++) {
-    const int buf = buf_of(k);
-    const long long next = tile + gridDim.x;
-    if (tid == 0) {
-      if (ok && a.nbuf == 2 && next < a.ntiles) {   // the other buffer's MMAs finished with the previous tile
-        issue_halo(next, buf_of(k + 1));
-        halo_issued++;
-      }
-      if (ok && k == 0) ok = mbar_wait_bounded(smem_u32(&bar[0]), 0, a.err, kErrFullWait);
-      if (ok) ok = mbar_wait_bounded(smem_u32(&bar[1 + buf]), par_of(k), a.err, kErrFullWait);
-      if (ok) {
-        halo_used++;
+  if (warp == 4) {
+    // ---------------- producer: TMA and MMA issue ----------------
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16(kTM, a.np, false, false);
+      const int ngn = a.np / 8;
+      auto issue_halo = [&](int k) {
+        int n, z, y0, x0;
+        tile_pos(k, n, z, y0, x0);
+        const uint32_t fb = smem_u32(&full[hbuf(k)]);
+        mbar_arrive_expect_tx(fb, (uint32_t)ngh * (kHaloX * kHaloY * kHaloZ * 16));
+        const uint32_t dst = smem_u32(halo + hbuf(k) * hbytes);
+        for (int g = 0; g < ngh; g++)
+          tma_load_5d(dst + g * kHaloGS, &tmx, 8 * g, x0 - 1, y0 - 1, z - 1, n, fb);
+      };
+      prefetch_tmap(&tmx);
+      mbar_arrive_expect_tx(smem_u32(wbar), a.wbytes);
+      bulk_load(smem_u32(wsm), wp, a.wbytes, smem_u32(wbar));
+      int issued = 0;
+      for (; issued < a.nbuf && issued < ntile; issued++) issue_halo(issued);
+      bool ok = mbar_wait_bounded(smem_u32(wbar), 0, a.err, kErrFullWait);
+      int k = 0;
+      for (; ok && k < ntile; k++) {
+        if (*abort_flag) { ok = false; break; }
+        // refill the buffer tile k-1 used, once its MMAs are done
+        if (k >= 1 && issued < ntile && hbuf(issued) == hbuf(k - 1)) {
+          if (!mbar_wait_bounded(smem_u32(&hfree[hbuf(k - 1)]), hpar(k - 1), a.err, kErrMmaWait)) { ok = false; break; }
+          issue_halo(issued++);
+        }
+        const int ab = k & 1;
+        if (!mbar_wait_bounded(smem_u32(&full[hbuf(k)]), hpar(k), a.err, kErrFullWait)) { ok = false; break; }
+        if (k >= 2 && !mbar_wait_bounded(smem_u32(&afree[ab]), ((k - 2) >> 1) & 1, a.err, kErrMmaWait)) { ok = false; break; }
         tc::fence_after_sync();
-        const uint32_t h0 = smem_u32(halo + buf * hbytes), w0 = smem_u32(wsm);
+        const uint32_t h0 = smem_u32(halo + hbuf(k) * hbytes), w0 = smem_u32(wsm);
+        const uint32_t d = tmem + ab * acols;
         bool first = true;
         for (int t = 0; t < 27; t++) {
           const int q = (t * 57) >> 9, r = t - 9 * q, q3 = (r * 11) >> 5;   // t = 9 dz' + 3 dy' + dx'
@@ -388,70 +407,73 @@ __global__ void __launch_bounds__(kUThreads) conv_halo_kernel(const __grid_const
             const uint64_t ad = tc::smem_desc(h0 + 2 * s * kHaloGS + tap_off, kHaloGS, kHaloX * 16);
             const uint64_t bd =
                 tc::smem_desc(w0 + (uint32_t)((t * ngc + 2 * s) * ngn * 128), ngn * 128, 128);
-            tc::mma_bf16(tmem, ad, bd, idesc, first ? 0u : 1u);
+            tc::mma_bf16(d, ad, bd, idesc, first ? 0u : 1u);
             first = false;
           }
         }
-        tc::mma_commit(smem_u32(&bar[3]));
+        tc::mma_commit(smem_u32(&accb[ab]));
+        tc::mma_commit(smem_u32(&hfree[hbuf(k)]));
+        // single buffer: the next halo can only start once these MMAs are done
       }
+      if (!ok) *abort_flag = 1;
+      // never leave with a copy in flight: wait for every halo issued (each
+      // was consumed above or is waited for here) and the weights
+      for (int i = k; i < issued; i++) mbar_wait_bounded(smem_u32(&full[hbuf(i)]), hpar(i), a.err, kErrDrainWait);
+      // and for the MMAs issued (the last commit covers all of them)
+      if (k > 0) mbar_wait_bounded(smem_u32(&hfree[hbuf(k - 1)]), hpar(k - 1), a.err, kErrDrainWait);
     }
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    if (!mbar_wait_bounded(smem_u32(&bar[3]), k & 1, a.err, kErrMmaWait)) ok = false;
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    tc::fence_after_sync();
-    if (tid == 0 && a.nbuf == 1 && next < a.ntiles) {   // the MMAs are done with the only buffer
-      issue_halo(next, 0);
-      halo_issued++;
-    }
-    // epilogue: TMEM lane = tile row r = 8 * (y - y0) + (x - x0)
-    int n, z, y0, x0;
-    tile_pos(tile, n, z, y0, x0);
-    const int r = warp * 32 + lane;
-    const int yy = y0 + (r >> 3), xx = x0 + (r & 7);
-    const bool vin = yy < a.H && xx < a.W;
-    const long long v = (((long long)n * a.D + z) * a.H + yy) * a.W + xx;
-    for (int n0 = 0; n0 < a.np; n0 += 16) {
-      float acc[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + n0, acc);
-      if (vin) {
+  } else {
+    // ---------------- epilogue warps 0-3 ----------------
+    const int r = warp * 32 + lane;   // tile row = tensor-memory lane
+    for (int k = 0; k < ntile; k++) {
+      const int ab = k & 1;
+      bool ok = mbar_wait_bounded(smem_u32(&accb[ab]), (k >> 1) & 1, a.err, kErrMmaWait);
+      if (!__all_sync(0xffffffffu, ok) || *abort_flag) {   // tensor-memory loads are warp-wide
+        *abort_flag = 1;
+        break;
+      }
+      tc::fence_after_sync();
+      int n, z, y0, x0;
+      tile_pos(k, n, z, y0, x0);
+      const int yy = y0 + (r >> 3), xx = x0 + (r & 7);
+      const bool vin = yy < a.H && xx < a.W;
+      const long long v = (((long long)n * a.D + z) * a.H + yy) * a.W + xx;
+      for (int n0 = 0; n0 < a.np; n0 += 16) {
+        float acc[16];
+        tc::tmem_ld16(tmem + ab * acols + ((uint32_t)(warp * 32) << 16) + n0, acc);
+        if (vin) {
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
-          const int c = n0 + i;
-          float o = acc[i] + ((c < a.cout && a.bias) ? a.bias[c] : 0.f);
-          if (a.relu) o = fmaxf(o, 0.f);
-          acc[i] = o;
-        }
-        if (a.y) {
+          for (int i = 0; i < 16; i++) {
+            const int c = n0 + i;
+            float o = acc[i] + ((c < a.cout && a.bias) ? a.bias[c] : 0.f);
+            if (a.relu) o = fmaxf(o, 0.f);
+            acc[i] = o;
+          }
+          if (a.y) {
 #pragma unroll
-          for (int i = 0; i < 16; i += 8) {
-            if (n0 + i + 8 <= a.cout) {
-              __align__(16) __nv_bfloat16 h[8];
+            for (int i = 0; i < 16; i += 8) {
+              if (n0 + i + 8 <= a.cout) {
+                __align__(16) __nv_bfloat16 h[8];
 #pragma unroll
-              for (int e = 0; e < 8; e++) h[e] = __float2bfloat16_rn(acc[i + e]);
-              *reinterpret_cast<uint4 *>(a.y + v * a.y_cstride + a.y_coff + n0 + i) =
-                  *reinterpret_cast<const uint4 *>(h);
+                for (int e = 0; e < 8; e++) h[e] = __float2bfloat16_rn(acc[i + e]);
+                *reinterpret_cast<uint4 *>(a.y + v * a.y_cstride + a.y_coff + n0 + i) =
+                    *reinterpret_cast<const uint4 *>(h);
+              }
             }
           }
-        }
-        if (a.yf) {
+          if (a.yf) {
 #pragma unroll
-          for (int i = 0; i < 16; i++)
-            if (n0 + i < a.cout)
-              a.yf[v * a.cout + n0 + i] = acc[i] + (a.resid ? a.resid[v * a.cout + n0 + i] : 0.f);
+            for (int i = 0; i < 16; i++)
+              if (n0 + i < a.cout)
+                a.yf[v * a.cout + n0 + i] = acc[i] + (a.resid ? a.resid[v * a.cout + n0 + i] : 0.f);
+          }
         }
       }
+      // this warp has read accumulator ab: the producer may overwrite it
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&afree[ab]));
     }
-    // the accumulator is read: the next tile's MMAs may overwrite it
-    tc::fence_before_sync();
-    __syncthreads();
-  }
-  // never leave with a copy in flight (an error path may have skipped waits)
-  if (tid == 0) {
-    if (halo_used == 0 && halo_issued > 0) mbar_wait_bounded(smem_u32(&bar[0]), 0, a.err, kErrDrainWait);
-    for (int i = halo_used; i < halo_issued; i++)
-      mbar_wait_bounded(smem_u32(&bar[1 + buf_of(i)]), par_of(i), a.err, kErrDrainWait);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -862,9 +884,9 @@ int check_conv_args(int cin, int cstride, int coff, int cout, int ntap) {
 int np_of(int cout) { return ((cout + 15) / 16) * 16; }
 
 // The halo-staged convolution takes 3x3x3 layers whose planes hold at least
-// one 16 x 8 tile and whose weights and a halo buffer fit in 200 KB of shared
-// memory (one CTA per SM for the largest of them).
-constexpr size_t kHaloMaxSmem = 200 * 1024;
+// one 16 x 8 tile and whose weights and a halo buffer fit in the 227 KB of
+// shared memory a CTA may have (one CTA per SM for the largest of them).
+constexpr size_t kHaloMaxSmem = 227 * 1024;
 bool g_halo_enabled = true;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
@@ -937,12 +959,12 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
     if (e != cudaSuccess) return set_error("unet conv: %s", cudaGetErrorString(e));
     attr = true;
   }
-  // tensor memory: at most 512 columns per SM across resident CTAs
-  const int ncols = np <= 32 ? 32 : (np <= 64 ? 64 : 128);
+  // tensor memory: two accumulators per CTA, at most 512 columns per SM
+  const int ncols = 2 * (np <= 32 ? 32 : (np <= 64 ? 64 : 128));
   if (per_sm * ncols > 512) per_sm = 512 / ncols;
   long long grid = (long long)g_num_sms * per_sm;
   if (grid > a.ntiles) grid = a.ntiles;
-  conv_halo_kernel<<<(unsigned)grid, kUThreads, smem, st>>>(tm, (const __nv_bfloat16 *)wpacked, a);
+  conv_halo_kernel<<<(unsigned)grid, kHaloThreads, smem, st>>>(tm, (const __nv_bfloat16 *)wpacked, a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
 }

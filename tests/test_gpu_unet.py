@@ -213,7 +213,9 @@ def test_training_reduces_loss(net):
 HALO_CASES = [(2, 8, 24, 20, 16, 16, 0), (1, 6, 32, 16, 32, 48, 0), (1, 5, 16, 8, 48, 16, 1),
               (1, 4, 17, 9, 16, 32, 1), (2, 3, 16, 24, 32, 32, 0),
               # odd channel-group counts (one zero group in the halo)
-              (2, 4, 16, 8, 8, 16, 0), (1, 3, 20, 12, 24, 16, 0), (1, 3, 16, 16, 24, 32, 1)]
+              (2, 4, 16, 8, 8, 16, 0), (1, 3, 20, 12, 24, 16, 0), (1, 3, 16, 16, 24, 32, 1),
+              # the widest layer that fits (weights 135 KB + one 85 KB halo)
+              (1, 3, 16, 16, 80, 32, 0)]
 
 
 @pytest.mark.parametrize("nb,D,H,W,cin,cout,tr", HALO_CASES)
@@ -266,7 +268,7 @@ def test_halo_conv_speed_384(net):
     stream = torch.cuda.ExternalStream(st)
     D = H = W = 384
     res = {}
-    for cin, cout in ((8, 16), (16, 16), (32, 32), (48, 16)):
+    for cin, cout in ((8, 16), (16, 16), (32, 32), (48, 16), (80, 32)):
         g = torch.Generator(device="cuda").manual_seed(cin)
         x = torch.randn(D * H * W * cin, device="cuda", generator=g).to(torch.bfloat16)
         wt = torch.randn(27 * cin * cout, device="cuda", generator=g) * 0.05
