@@ -40,7 +40,7 @@ int sepx_batch_rtm_adjoint(int jt, int npts, int nt, int how);
  * keep the fastest (clears every shot's receiver traces) */
 int sepx_batch_autotune(int jt, int npts_src, int nsteps, int *zchunk, int *stages, int *style,
                         float *best_ms);
-/* zchunk 0: the single-shot default; stages 3 or 4; style 0 or 1 */
+/* zchunk 0: the single-shot default; stages 2, 3 or 4; style 0 or 1 */
 int sepx_batch_set_tuning(int zchunk, int stages, int style);
 int sepx_batch_get_tuning(int *zchunk, int *stages, int *style);
 

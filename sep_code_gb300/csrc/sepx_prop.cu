@@ -27,6 +27,7 @@
 // __fmaf_rn / __fmul_rn / __fadd_rn, no contraction freedom), so a step is
 // bit-identical to the CPU restatement.
 #include <cuda.h>
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -37,9 +38,10 @@
 
 // Resident CTAs per SM the register budget targets, and ring depths, of the
 // two heaviest modes (compile-time tuning knobs; the defaults measured best
-// on GB300 at 560x560x496).
+// on GB300 at 560x560x496: the Born forward with its z-queues in tensor
+// memory, 96 registers and a 2-stage ring runs 4 CTAs per SM).
 #ifndef SEPX_FWD_MINB
-#define SEPX_FWD_MINB 3
+#define SEPX_FWD_MINB 4
 #endif
 #ifndef SEPX_ADJ_MINB
 #define SEPX_ADJ_MINB 3
@@ -47,10 +49,10 @@
 // 1: the z-queues of the Born forward live in tensor memory (tcgen05.ld/st)
 // instead of registers
 #ifndef SEPX_TMEMQ
-#define SEPX_TMEMQ 0
+#define SEPX_TMEMQ 1
 #endif
 #ifndef SEPX_FWD_STAGES
-#define SEPX_FWD_STAGES 3
+#define SEPX_FWD_STAGES 2
 #endif
 #ifndef SEPX_ADJ_STAGES
 #define SEPX_ADJ_STAGES 3
@@ -769,9 +771,16 @@ __global__ void __launch_bounds__(kThreads, batch_minb<MODE>())
   tq_free<MODE>(tq);
 }
 
-// Up to kMaxMulti grids in one launch, parameters in parameter space.
+// Up to kMaxMulti grids in one launch, parameters in parameter space.  The
+// per-CTA grid lookup costs registers: the Born forward keeps the budget of 3
+// CTAs per SM here (96 registers spill).
+template <int MODE>
+constexpr int multi_minb() {
+  return MODE == kBornFwd ? 3 : Mode<MODE>::MINB;
+}
+
 template <int MODE, int STAGES>
-__global__ void __launch_bounds__(kThreads, Mode<MODE>::MINB)
+__global__ void __launch_bounds__(kThreads, multi_minb<MODE>())
     prop_multi_kernel(const __grid_constant__ MultiParams mp) {
   extern __shared__ unsigned char smem_raw[];
   const int b = blockIdx.x;
@@ -859,19 +868,37 @@ static cudaError_t launch_batch_mode(const PropParams *params, const int4 *items
   return cudaGetLastError();
 }
 
+// Resident CTAs per SM of the persistent kernel, from its registers and
+// shared memory (every CTA of its grid must be resident at once), and for the
+// tensor-memory z-queue modes from the 512 columns of an SM.
 template <int MODE, int STAGES>
 static int batch_occupancy_mode() {
   const size_t smem = batch_smem_bytes_of<MODE, STAGES>();
   auto kern = prop_batch_kernel<MODE, STAGES>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kThreads, smem) != cudaSuccess) return 0;
-  return n;
+  cudaFuncAttributes fa;
+  int dev = 0, smem_sm = 0, resv = 0, regs_sm = 0, thr_sm = 0;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess)
+    return 0;
+  const size_t per_smem = ((smem + fa.sharedSizeBytes + 127) / 128) * 128 + (size_t)resv;
+  // registers are allocated per warp in units of 256
+  const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+  const int per_regs = warp_regs * (kThreads / 32);
+  int n = (int)((size_t)smem_sm / per_smem);
+  n = std::min(n, regs_sm / std::max(per_regs, 1));
+  n = std::min(n, thr_sm / kThreads);
+  if (Mode<MODE>::TQ) n = std::min(n, (int)(512 / Mode<MODE>::TQ_COLS));
+  return std::max(n, 0);
 }
 
-#define SEPX_BATCH_CASES(X) \
-  X(kSrcProp, 3) X(kSrcProp, 4) X(kBornFwd, 3) X(kBornFwd, 4) X(kRtmAdj, 3) X(kRtmAdj, 4) X(kRtmAdj1, 3)
+#define SEPX_BATCH_CASES(X)                                                                  \
+  X(kSrcProp, 3) X(kSrcProp, 4) X(kBornFwd, 2) X(kBornFwd, 3) X(kBornFwd, 4) X(kRtmAdj, 3) \
+  X(kRtmAdj, 4) X(kRtmAdj1, 3)
 
 cudaError_t launch_prop_multi(int mode, int stages, const MultiParams &mp, cudaStream_t st) {
 #define X(m, s) if (mode == m && stages == s) return launch_multi_mode<m, s>(mp, st);
