@@ -349,10 +349,13 @@ def run_ours(args, ws, rank, dist):
 
         e2e_step()   # warm
         barrier(dist)
+        e2e_clocks = ClockSampler()
+        e2e_clocks.start()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             e2e_step()
         e_el = max_over_ranks(dist, time.perf_counter() - t0)
+        e2e_clk = e2e_clocks.stop()
         vb = 4 * n1 * n2 * n3
         tb = 4 * nrec * st.nt_big
         h2d = 3 * vb + vb + 2 * vb + 2 * tb + 4 * (h_v9.size + 2 * h_v8.size)
@@ -361,7 +364,8 @@ def run_ours(args, ws, rank, dist):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": round(e_el / args.steps * 1e3, 2),
                "path": "reference-named C ABI (sepx_source_prop / sepx_rtm_forward / "
-                       "sepx_rtm_adjoint) with pinned host buffers"}
+                       "sepx_rtm_adjoint) with pinned host buffers",
+               "clocks": e2e_clk}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
