@@ -69,25 +69,54 @@ def patch_survey(vel, refl, d, nt, f0=15.0):
 
 
 def make_pairs(npairs: int, n: int = 64, nt: int = 1100, d: float = 12.5, nvel: int = 20,
-               seed: int = 20261207, snap_js: int = 4, verbose: bool = False):
-    """(x, m) pairs, x = L'L m, both [npairs, n, n, n] FP32 numpy, unit RMS each."""
+               seed: int = 20261207, snap_js: int = 4, iterates: int = 0, verbose: bool = False):
+    """(x, m) pairs, x = L'L m, both [npairs, n, n, n] FP32 numpy, unit RMS each.
+
+    iterates > 0: each random reflectivity m also yields the pairs (g_k, e_k)
+    of that many steepest-descent iterates m_k on |L m_k - L m|^2 (exact line
+    search): e_k = m - m_k is the remaining error and g_k = L'(L m - L m_k) =
+    L'L e_k the gradient there -- the inputs the solver hands the network after
+    its first iteration.  Each pair costs one forward and one adjoint."""
     rng = np.random.default_rng(seed)
     X = np.zeros((npairs, n, n, n), np.float32)
     Y = np.zeros((npairs, n, n, n), np.float32)
     per = (npairs + nvel - 1) // nvel
     k = 0
     t0 = time.perf_counter()
+
+    def put(x, m):
+        nonlocal k
+        X[k] = x / max(np.sqrt(np.mean(x.astype(np.float64) ** 2)), 1e-30)
+        Y[k] = m / max(np.sqrt(np.mean(m.astype(np.float64) ** 2)), 1e-30)
+        k += 1
+
     while k < npairs:
         vel = velocity_model(rng, (n, n, n), d)
         s = patch_survey(vel, np.zeros_like(vel), d, nt)
         op = RtmOperator(s, mode="linear", snap_js=snap_js, snap_prec="f32")
         try:
-            for _ in range(min(per, npairs - k)):
+            done = 0
+            while done < per and k < npairs:
                 m = random_reflectivity(rng, (n, n, n))
-                x = op.adjoint(op.forward(m))
-                X[k] = x / max(np.sqrt(np.mean(x.astype(np.float64) ** 2)), 1e-30)
-                Y[k] = m / max(np.sqrt(np.mean(m.astype(np.float64) ** 2)), 1e-30)
-                k += 1
+                r = op.forward(m)            # residual of m_0 = 0: d - L m_0 = L m
+                g = op.adjoint(r)
+                put(g, m)
+                done += 1
+                mk = np.zeros_like(m)
+                for _ in range(iterates):
+                    if k >= npairs or done >= per:
+                        break
+                    lg = op.forward(g)
+                    gg = float(np.dot(g.ravel().astype(np.float64), g.ravel()))
+                    ll = float(np.dot(lg.ravel().astype(np.float64), lg.ravel()))
+                    if not (ll > 0):
+                        break
+                    a = gg / ll
+                    mk = (mk + a * g).astype(np.float32)
+                    r = (r - a * lg).astype(np.float32)
+                    g = op.adjoint(r)
+                    put(g, m - mk)
+                    done += 1
         finally:
             op.close()
         if verbose:
@@ -275,6 +304,8 @@ def main(argv=None):
     t.add_argument("--batch", type=int, default=4)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--out", default=str(WEIGHTS))
+    t.add_argument("--iterates", type=int, default=0,
+                   help="also train on this many steepest-descent iterates per reflectivity")
     c = sub.add_parser("lsrtm")
     c.add_argument("--n", type=int, default=384)
     c.add_argument("--nt", type=int, default=3000)
@@ -289,14 +320,15 @@ def main(argv=None):
     a = p.parse_args(argv)
     if a.cmd == "train":
         t0 = time.perf_counter()
-        X, Y = make_pairs(a.pairs, n=a.n, nt=a.nt, verbose=True)
+        X, Y = make_pairs(a.pairs, n=a.n, nt=a.nt, iterates=a.iterates, verbose=True)
         t1 = time.perf_counter()
         net = UNet3D(seed=0)
         hist = train(net, X, Y, epochs=a.epochs, batch=a.batch, lr=a.lr, verbose=True)
         t2 = time.perf_counter()
         Path(a.out).parent.mkdir(parents=True, exist_ok=True)
         net.save(a.out)
-        print(json.dumps({"pairs": a.pairs, "patch": a.n, "nt": a.nt, "seconds_pairs": t1 - t0,
+        print(json.dumps({"pairs": a.pairs, "iterates": a.iterates, "patch": a.n, "nt": a.nt,
+                          "seconds_pairs": t1 - t0,
                           "seconds_training": t2 - t1, "epochs": a.epochs, "loss": hist}))
     else:
         s = lsrtm_survey(a.n, a.nt, a.shots)

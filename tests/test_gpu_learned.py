@@ -83,3 +83,28 @@ def test_adaptive_direction_policy_and_target_stop():
         assert len(rs) == 6 and np.allclose(rs, rp[:6], rtol=0, atol=0)
     finally:
         op.close()
+
+
+def test_descent_iterate_pairs_are_normal_equation_pairs():
+    """make_pairs(iterates=2): every input is L'L applied to its target (up to
+    the unit-RMS normalisation of each): the descent iterates' gradients are
+    the normal operator of the remaining error"""
+    from sep_code_gb300 import learned as Lr
+    from sep_code_gb300.operator import RtmOperator
+    X, Y = Lr.make_pairs(3, n=32, nt=400, nvel=1, seed=5, iterates=2)
+    assert np.all(np.isfinite(X)) and np.all(np.isfinite(Y))
+    # the same velocity model the generator drew (first draw of its rng)
+    rng = np.random.default_rng(5)
+    vel = Lr.velocity_model(rng, (32, 32, 32), 12.5)
+    s = Lr.patch_survey(vel, np.zeros_like(vel), 12.5, 400)
+    op = RtmOperator(s, mode="linear", snap_js=4, snap_prec="f32")
+    try:
+        for k in range(3):
+            want = op.adjoint(op.forward(Y[k]))
+            want = want / np.sqrt(np.mean(want.astype(np.float64) ** 2))
+            err = np.linalg.norm((X[k] - want).astype(np.float64)) / np.linalg.norm(want.astype(np.float64))
+            assert err <= 1e-3, (k, err)
+        # the iterates are different problems: the error shrinks its low-frequency part
+        assert np.linalg.norm(X[1] - X[0]) > 1e-2 * np.linalg.norm(X[0])
+    finally:
+        op.close()
