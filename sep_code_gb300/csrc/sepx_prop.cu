@@ -380,8 +380,10 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
         // tensor-memory operations are warp-wide: leave the loop together
         if (!__all_sync(0xffffffffu, ok)) break;
         tc::tmem_wait_st();   // the previous plane's feed is in place
-#pragma unroll
-        for (int f = 0; f < NF; f++) tc::tmem_ld32_q8(tq + f * 64 + 4 * (i & 7), q[f]);
+        if (NF == 2)
+          tc::tmem_ld32_q8_pair(tq + 4 * (i & 7), tq + 64 + 4 * (i & 7), q[0], q[NF - 1]);
+        else
+          tc::tmem_ld32_q8(tq + 4 * (i & 7), q[0]);
         q[0][8] = q[NF - 1][8] = make_float4(0.f, 0.f, 0.f, 0.f);
       } else if (!ok) {
         break;
