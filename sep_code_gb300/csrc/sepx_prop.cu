@@ -51,6 +51,10 @@
 #ifndef SEPX_TMEMQ
 #define SEPX_TMEMQ 1
 #endif
+// 1: the RTM adjoint's z-queues in tensor memory as well
+#ifndef SEPX_TMEMQ_ADJ
+#define SEPX_TMEMQ_ADJ 0
+#endif
 #ifndef SEPX_FWD_STAGES
 #define SEPX_FWD_STAGES 2
 #endif
@@ -103,7 +107,7 @@ struct Mode {
   // 16 slots of 4 columns (planes w and w+8 of a ring of 8, so the 8 planes
   // z-4 .. z+3 of every step are 32 consecutive columns); the z+4 feed is
   // read from shared memory and written to both copies of its slot
-  static constexpr bool TQ = SEPX_TMEMQ && MODE == kBornFwd;
+  static constexpr bool TQ = (SEPX_TMEMQ && MODE == kBornFwd) || (SEPX_TMEMQ_ADJ && MODE == kRtmAdj);
   static constexpr uint32_t TQ_COLS = NF == 2 ? 128u : 64u;
   // resident blocks per SM the register budget is sized for
   static constexpr int MINB = (MODE == kSrcProp)  ? 4
