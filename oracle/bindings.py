@@ -1,4 +1,4 @@
-"""ctypes bindings for the checker libraries (test infrastructure only).
+"""ctypes bindings for the oracle libraries (test infrastructure only).
 
 ``Oracle`` wraps oracle/_build/libsepx_oracle.so (the CPU restatement);
 ``RefHost`` wraps oracle/_ref/libsepref.so (the reference's own host C++).

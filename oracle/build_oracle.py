@@ -1,4 +1,4 @@
-"""Build recipe for the checker libraries under oracle/ (test infrastructure).
+"""Build recipe for the oracle libraries under oracle/ (test infrastructure).
 
 * ``oracle/_build/libsepx_oracle.so`` -- the CPU restatement (sepx_oracle.c).
 * ``oracle/_ref/libsepref.so`` -- the reference's own host C++ (sinc tables,

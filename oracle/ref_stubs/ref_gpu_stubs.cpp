@@ -1,5 +1,5 @@
 // CPU stand-in for the reference's GPU C-ABI (Born/gpu_funcs_3d.h), linked into
-// the checker library so that the reference's own host classes (rtm_zero_op,
+// the oracle's reference library so that the reference's own host classes (rtm_zero_op,
 // fd_prop, ...) run end to end on the CPU.  Each entry point keeps the
 // reference's module-global state and semantics and runs the propagation
 // loops of the oracle (sepx_oracle.c).  Every call is also recorded so tests

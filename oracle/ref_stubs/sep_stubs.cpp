@@ -1,6 +1,6 @@
 // In-memory stand-ins for the SEPlib calls made by the reference's host C++,
 // so that its classes (vel_fd_3d, source_func, data_rtm_3d, image_rtm_3d,
-// oc_float, rtm_zero_op, ...) run unchanged inside the checker library
+// oc_float, rtm_zero_op, ...) run unchanged inside the oracle's reference library
 // oracle/_ref/libsepref.so.  A "file" is a named byte buffer with a cursor and
 // SEP-style axes; parameters are a name->string table.  Test infrastructure.
 #include <cstdarg>
@@ -108,10 +108,10 @@ FILE *auxout(const char *tag) { (void)file(tag); return stderr; }
 int auxclose(const char *) { return 0; }
 
 int sreed_window(const char *, int *, int *, int *, int *, int *, int, void *) {
-  return seperr("sreed_window is not available in the checker\n");
+  return seperr("sreed_window is not available in the oracle's reference library\n");
 }
 int srite_window(const char *, int *, int *, int *, int *, int *, int, void *) {
-  return seperr("srite_window is not available in the checker\n");
+  return seperr("srite_window is not available in the oracle's reference library\n");
 }
 
 int sep_get_number_data_axes(const char *tag, int *n) {
@@ -146,7 +146,7 @@ void initpar(int, char **) {}
 
 // oc_float::make_temp (Born/oc_float.cpp:406-412) names temporary datasets
 // with mkstemp, which would create files in the working directory: the
-// checker's datasets live in memory, so this library's own calls get a
+// oracle's datasets live in memory, so this library's own calls get a
 // unique name and no file (no descriptor is returned; the reference ignores it).
 int mkstemp(char *tmpl) {
   static unsigned long long counter = 0;
@@ -156,7 +156,7 @@ int mkstemp(char *tmpl) {
   return -1;
 }
 
-// ---- registry access for the checker ----
+// ---- registry access for the oracle ----
 void ref_reset(void) { g_files.clear(); g_params.clear(); }
 
 void ref_file_put(const char *tag, int ndim, const int *n, const float *o, const float *d,

@@ -1,5 +1,5 @@
 /* Declarations standing in for SEPlib's seplib.h, so that the reference's host
- * C++ compiles for the checker library (oracle/_ref).  Test infrastructure only.
+ * C++ compiles for the oracle's reference library (oracle/_ref).  Test infrastructure only.
  * The file-backed calls are served from an in-memory registry (sep_stubs.cpp). */
 #ifndef SEPX_REF_SEPLIB_STUB_H
 #define SEPX_REF_SEPLIB_STUB_H

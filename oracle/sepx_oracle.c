@@ -1,6 +1,6 @@
 /*
  * sepx_oracle.c -- CPU restatement of SEP_Code's acoustic Born/RTM path.
- * TEST INFRASTRUCTURE ONLY: the parity checker and the timed CPU baseline.
+ * TEST INFRASTRUCTURE ONLY: the parity oracle and the timed CPU baseline.
  * Build: oracle/build_oracle.py (C11, -O3 -fopenmp -ffp-contract=off).
  */
 #include "sepx_oracle.h"

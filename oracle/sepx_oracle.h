@@ -1,7 +1,7 @@
 /*
  * sepx_oracle.h -- CPU restatement of SEP_Code's 3D acoustic Born/RTM path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the CUDA
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity oracle for the CUDA
  * path in sep_code_gb300/ and the timed CPU baseline of bench.py.  Nothing in
  * the product links, imports or calls it.
  *

@@ -12,8 +12,8 @@
 //  * axes: n1.. (missing: 1), o1.. (0), d1.. (1), label1.. (""); the number of
 //    axes is the largest i with n_i given and n_i > 1 (at least 1);
 //  * data: esize=4, data_format="xdr_float" (big-endian IEEE single, the SEP
-//    default) or "native_float" (little-endian on every host this builds
-//    for), axis 1 fastest; in= is the data file (a relative path is looked
+//    default) or "native_float" (little-endian on every host this library
+//    is compiled for), axis 1 fastest; in= is the data file (a relative path is looked
 //    up beside the header first, then from the working directory; written
 //    headers name the data file by its absolute path).
 // Device transfers go through two pinned staging buffers on the library's

@@ -11,7 +11,7 @@
   ``RtmOperator.lsrtm`` (simple_solver + cgstep, Born/lin_solver.cpp:115-143)
   applies before the forward product.  cgstep's two-term plane search
   (Born/cgstep.cpp:14-58) keeps the data residual non-increasing for any
-  direction, so plain CG remains the judge of what the network buys.
+  direction, so plain CG remains the yardstick of what the network buys.
 """
 from __future__ import annotations
 

@@ -1,6 +1,6 @@
 """The linearised Born pair (least-squares RTM operator): GPU vs oracle with
 FP32 / BF16 / FP16 source snapshots, and the adjoint dot-product test
-<L m, d> = <m, L' d> to 1e-6 relative (spec tolerance), FP64 sums."""
+<L m, d> = <m, L' d> to 1e-6 relative, FP64 sums."""
 import numpy as np
 import pytest
 

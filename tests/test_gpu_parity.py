@@ -1,6 +1,6 @@
 """CUDA path vs the oracle on the same seeded shots, through the C ABI.
 
-Tolerance: the spec bar is relative L2 <= 1e-5 on FP32 traces and
+Tolerance: relative L2 <= 1e-5 on FP32 traces and
 images after the full time loop.  The kernels and the oracle share one
 floating-point contract (explicit fused multiply-adds in the reference's term
 order, shared sponge table), so the results are also expected to be
