@@ -55,6 +55,18 @@
 #ifndef SEPX_TMEMQ_ADJ
 #define SEPX_TMEMQ_ADJ 0
 #endif
+// the linearised forward: z-queues in tensor memory, CTAs per SM, ring depth
+// (tensor memory frees the registers for 3 CTAs per SM: the forward pass of
+// the linearised pair on 256^3 x 1500 steps 0.393 -> 0.386 s)
+#ifndef SEPX_TMEMQ_LIN
+#define SEPX_TMEMQ_LIN 1
+#endif
+#ifndef SEPX_LINFWD_MINB
+#define SEPX_LINFWD_MINB 3
+#endif
+#ifndef SEPX_LINFWD_STAGES
+#define SEPX_LINFWD_STAGES 3
+#endif
 #ifndef SEPX_FWD_STAGES
 #define SEPX_FWD_STAGES 2
 #endif
@@ -107,13 +119,14 @@ struct Mode {
   // 16 slots of 4 columns (planes w and w+8 of a ring of 8, so the 8 planes
   // z-4 .. z+3 of every step are 32 consecutive columns); the z+4 feed is
   // read from shared memory and written to both copies of its slot
-  static constexpr bool TQ = (SEPX_TMEMQ && MODE == kBornFwd) || (SEPX_TMEMQ_ADJ && MODE == kRtmAdj);
+  static constexpr bool TQ = (SEPX_TMEMQ && MODE == kBornFwd) || (SEPX_TMEMQ_ADJ && MODE == kRtmAdj) ||
+                              (SEPX_TMEMQ_LIN && MODE == kLinFwd);
   static constexpr uint32_t TQ_COLS = NF == 2 ? 128u : 64u;
   // resident blocks per SM the register budget is sized for
   static constexpr int MINB = (MODE == kSrcProp)  ? 4
                               : (MODE == kBornFwd) ? SEPX_FWD_MINB
                               : (MODE == kRtmAdj)  ? SEPX_ADJ_MINB
-                              : (MODE == kLinFwd)  ? 2
+                              : (MODE == kLinFwd)  ? SEPX_LINFWD_MINB
                                                    : 3;
 };
 
@@ -367,8 +380,7 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
             if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, ldg4(P.vel + off));
           }
           if (M::TQ) {
-            tc::tmem_st4(tq + f * 64 + 4 * j, p);
-            tc::tmem_st4(tq + f * 64 + 4 * (j + 8), p);
+            tc::tmem_st4x2_sync(tq + f * 64 + 4 * j, tq + f * 64 + 4 * (j + 8), p);
           } else {
             q[f][j] = p;
           }
@@ -383,7 +395,7 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
       if (M::TQ) {
         // tensor-memory operations are warp-wide: leave the loop together
         if (!__all_sync(0xffffffffu, ok)) break;
-        tc::tmem_wait_st();   // the previous plane's feed is in place
+        // the previous plane's feed is in place (its stores were waited for)
         if (NF == 2)
           tc::tmem_ld32_q8_pair(tq + 4 * (i & 7), tq + 64 + 4 * (i & 7), q[0], q[NF - 1]);
         else
@@ -661,12 +673,11 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
         // the z+4 plane replaces z-4 (slot i & 7 and its copy)
 #pragma unroll
         for (int f = 0; f < NF; f++) {
-          tc::tmem_st4(tq + f * 64 + 4 * (i & 7), q[f][8]);
-          tc::tmem_st4(tq + f * 64 + 4 * ((i & 7) + 8), q[f][8]);
+          tc::tmem_st4x2_sync(tq + f * 64 + 4 * (i & 7), tq + f * 64 + 4 * ((i & 7) + 8), q[f][8]);
         }
       }
     }
-    if (M::TQ) tc::tmem_wait_st();   // each warp owns its lanes: no barrier needed
+    // every tensor-memory store above completed before its registers were released
   }
 
   // Drain: never leave the CTA with bulk copies still writing its shared memory.
@@ -716,7 +727,8 @@ __device__ __forceinline__ void tq_free(uint32_t base) {
 }
 
 // the 4-float block-max slot of the carve holds the tensor-memory address
-// (the TQ modes do not use the block max)
+// (a TQ mode that later uses the block max, the linearised forward, has read
+// the address into a register before its first block max)
 template <int MODE, int STAGES>
 __device__ __forceinline__ float *tq_slot(float *smem) {
   return reinterpret_cast<float *>(reinterpret_cast<unsigned long long *>(
@@ -836,7 +848,7 @@ cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
     case kRtmAdj: return launch_mode<kRtmAdj, SEPX_ADJ_STAGES>(P, grid, st);
     case kRtmAdj1: return launch_mode<kRtmAdj1, 3>(P, grid, st);
     case kLinSrc: return launch_mode<kLinSrc, 4>(P, grid, st);
-    case kLinFwd: return launch_mode<kLinFwd, 3>(P, grid, st);
+    case kLinFwd: return launch_mode<kLinFwd, SEPX_LINFWD_STAGES>(P, grid, st);
     case kLinAdj: return launch_mode<kLinAdj, 3>(P, grid, st);
     default: return cudaErrorInvalidValue;
   }
@@ -943,7 +955,7 @@ size_t prop_smem_bytes(int mode) {
     case kRtmAdj: return smem_bytes_of<kRtmAdj, SEPX_ADJ_STAGES>();
     case kRtmAdj1: return smem_bytes_of<kRtmAdj1, 3>();
     case kLinSrc: return smem_bytes_of<kLinSrc, 4>();
-    case kLinFwd: return smem_bytes_of<kLinFwd, 3>();
+    case kLinFwd: return smem_bytes_of<kLinFwd, SEPX_LINFWD_STAGES>();
     case kLinAdj: return smem_bytes_of<kLinAdj, 3>();
   }
   return 0;

@@ -164,6 +164,19 @@ __device__ __forceinline__ void tmem_ld32_q8_pair(uint32_t a0, uint32_t a1, floa
                         __uint_as_float(r[32 + 4 * j + 2]), __uint_as_float(r[32 + 4 * j + 3]));
   }
 }
+// tcgen05.st reads its source registers asynchronously: they may be reused
+// only after tcgen05.wait::st.  Storing and waiting inside one asm statement
+// keeps the compiler from reusing them in between.  v goes to the 4 columns
+// at a0 and to the 4 at a1.
+__device__ __forceinline__ void tmem_st4x2_sync(uint32_t a0, uint32_t a1, float4 v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%2, %3, %4, %5};\n\t"
+      "tcgen05.st.sync.aligned.32x32b.x4.b32 [%1], {%2, %3, %4, %5};\n\t"
+      "tcgen05.wait::st.sync.aligned;" ::"r"(a0),
+      "r"(a1), "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
+      "r"(__float_as_uint(v.w))
+      : "memory");
+}
 __device__ __forceinline__ void tmem_st4(uint32_t taddr, float4 v) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr),
                "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
