@@ -66,9 +66,24 @@ def test_lin_dot_product_config1():
     """the 128^3, dx=10 m, dt=1 ms, 1000-step workload (padded 176x176x224)"""
     s = M.config1_survey()
     st = M.prepare_shot(s)
-    a, b = _dot_test(LinCase(s, st), 1, "f32")
+    c = LinCase(s, st)
+    a, b = _dot_test(c, 1, "f32")
     assert abs(a) > 0
     assert abs(a - b) / abs(a) <= 1e-6, (a, b)
+
+
+@pytest.mark.slow
+def test_lin_forward_repeatable_config1():
+    """the same forward twice on the 128^3 workload (several CTAs per SM
+    sharing tensor memory, 1000 steps): bit-identical traces"""
+    s = M.config1_survey()
+    st = M.prepare_shot(s)
+    c = LinCase(s, st)
+    m = np.random.default_rng(3).standard_normal((st.n[2], st.n[1], st.n[0])).astype(np.float32)
+    d1 = c.gpu_forward(m, 1, "bf16")
+    d2 = c.gpu_forward(m, 1, "bf16")
+    assert np.abs(d1).max() > 0
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
 
 
 def test_snapshot_memory(case):
