@@ -4,6 +4,9 @@
 // float operations of the reference's loops element by element.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
+
 #include "sepx_aux.h"
 
 namespace sepx {
@@ -172,6 +175,109 @@ __global__ void tmute_kernel(const float *__restrict__ in, float *__restrict__ o
   }
 }
 
+// The same three operations four columns at a time (16-byte loads and
+// stores), for rows whose lengths and offsets are multiples of 4 floats and
+// whose buffers are 16-byte aligned: a float4 group then lies wholly inside
+// or wholly outside the image.
+__device__ __forceinline__ float4 add4(float4 a, float4 b) {
+  return make_float4(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w));
+}
+
+__global__ void window_add4_kernel(float *__restrict__ img, int n1, int n2, int n3,
+                                   const float *__restrict__ sub, int s1, int s2, int s3, int f1,
+                                   int f2, int f3) {
+  const long long rows = (long long)s2 * s3;
+  const int q1 = s1 >> 2;
+  for (long long r = (long long)blockIdx.y * blockDim.y + threadIdx.y; r < rows;
+       r += (long long)gridDim.y * blockDim.y) {
+    const int i2 = (int)(r % s2), i3 = (int)(r / s2);
+    const int j2 = i2 + f2, j3 = i3 + f3;
+    if (j2 < 0 || j2 >= n2 || j3 < 0 || j3 >= n3) continue;   // uniform for the block row
+    float4 *orow = reinterpret_cast<float4 *>(img + (long long)n1 * (j2 + (long long)n2 * j3));
+    const float4 *irow = reinterpret_cast<const float4 *>(sub + (long long)s1 * r);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < q1; k += gridDim.x * blockDim.x) {
+      const int j1 = 4 * k + f1;
+      if (j1 >= 0 && j1 < n1) orow[j1 >> 2] = add4(orow[j1 >> 2], irow[k]);
+    }
+  }
+}
+
+__global__ void window_extract4_kernel(const float *__restrict__ img, const float *__restrict__ mute,
+                                       int n1, int n2, int n3, float *__restrict__ sub, int s1,
+                                       int s2, int s3, int f1, int f2, int f3) {
+  const long long rows = (long long)s2 * s3;
+  const int q1 = s1 >> 2;
+  for (long long r = (long long)blockIdx.y * blockDim.y + threadIdx.y; r < rows;
+       r += (long long)gridDim.y * blockDim.y) {
+    const int i2 = (int)(r % s2), i3 = (int)(r / s2);
+    const int j2 = i2 + f2, j3 = i3 + f3;
+    const bool row_in = j2 >= 0 && j2 < n2 && j3 >= 0 && j3 < n3;
+    const long long ro = (long long)n1 * (j2 + (long long)n2 * j3);
+    float4 *orow = reinterpret_cast<float4 *>(sub + (long long)s1 * r);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < q1; k += gridDim.x * blockDim.x) {
+      const int j1 = 4 * k + f1;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row_in && j1 >= 0 && j1 < n1) {
+        v = *reinterpret_cast<const float4 *>(img + ro + j1);
+        if (mute) {
+          const float4 m = *reinterpret_cast<const float4 *>(mute + ro + j1);
+          v = make_float4(__fmul_rn(v.x, m.x), __fmul_rn(v.y, m.y), __fmul_rn(v.z, m.z),
+                          __fmul_rn(v.w, m.w));
+        }
+      }
+      orow[k] = v;
+    }
+  }
+}
+
+__global__ void tmute4_kernel(const float *__restrict__ in, float *__restrict__ out, int add,
+                              float t0, float vmute, int n1, float o1, float d1, int n2, float o2,
+                              float d2, long long nrep) {
+  const long long rows = (long long)n2 * nrep;
+  const int q1 = n1 >> 2;
+  for (long long r = (long long)blockIdx.y * blockDim.y + threadIdx.y; r < rows;
+       r += (long long)gridDim.y * blockDim.y) {
+    const int i2 = (int)(r % n2);
+    const float tr = __fadd_rn(t0, __fdiv_rn(__fadd_rn(o2, __fmul_rn(d2, (float)i2)), vmute));
+    const float sf = __fdiv_rn(__fsub_rn(tr, o1), d1);
+    const int start = (sf >= (float)n1) ? n1 : max(0, __float2int_rz(sf));
+    const float4 *irow = reinterpret_cast<const float4 *>(in + (long long)n1 * r);
+    float4 *orow = reinterpret_cast<float4 *>(out + (long long)n1 * r);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < q1; k += gridDim.x * blockDim.x) {
+      const int i1 = 4 * k;
+      float4 v = add ? orow[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i1 + 3 >= start) {   // some column of the group passes
+        const float4 x = irow[k];
+        if (i1 >= start) v.x = __fadd_rn(v.x, x.x);
+        if (i1 + 1 >= start) v.y = __fadd_rn(v.y, x.y);
+        if (i1 + 2 >= start) v.z = __fadd_rn(v.z, x.z);
+        if (i1 + 3 >= start) v.w = __fadd_rn(v.w, x.w);
+      }
+      orow[k] = v;
+    }
+  }
+}
+
+static bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// 2-D blocks for the 16-byte kernels: x covers a row of q float4 (whole
+// warps, at most 256 threads), y takes as many rows as fill 256 threads
+struct RowsLaunch {
+  dim3 grid, block;
+};
+static RowsLaunch rows_launch4(int q, long long rows) {
+  int bx = ((std::max(q, 1) + 31) / 32) * 32;
+  if (bx > 256) bx = 256;
+  const int by = 256 / bx;
+  const int gx = std::min((q + bx - 1) / bx, 8);
+  long long gy = (rows + by - 1) / by;
+  if (gy > 2432) gy = 2432;
+  RowsLaunch L;
+  L.grid = dim3(std::max(gx, 1), (unsigned)std::max<long long>(gy, 1));
+  L.block = dim3(bx, by);
+  return L;
+}
+
 static dim3 rows_grid(int n1, long long rows) {
   // about 16 resident rows of 256 threads per SM on 152 SMs, x covering a row
   const int gx = (n1 + 255) / 256 < 8 ? (n1 + 255) / 256 : 8;
@@ -181,24 +287,40 @@ static dim3 rows_grid(int n1, long long rows) {
 
 cudaError_t launch_window_add(float *img, int n1, int n2, int n3, const float *sub, int s1, int s2,
                               int s3, int f1, int f2, int f3, cudaStream_t st) {
-  window_add_kernel<<<rows_grid(s1, (long long)s2 * s3), 256, 0, st>>>(img, n1, n2, n3, sub, s1, s2,
-                                                                       s3, f1, f2, f3);
+  if (n1 % 4 == 0 && s1 % 4 == 0 && f1 % 4 == 0 && al16(img) && al16(sub)) {
+    const RowsLaunch L = rows_launch4(s1 / 4, (long long)s2 * s3);
+    window_add4_kernel<<<L.grid, L.block, 0, st>>>(img, n1, n2, n3, sub, s1, s2, s3, f1, f2, f3);
+  } else {
+    window_add_kernel<<<rows_grid(s1, (long long)s2 * s3), 256, 0, st>>>(img, n1, n2, n3, sub, s1, s2,
+                                                                         s3, f1, f2, f3);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_window_extract(const float *img, const float *mute, int n1, int n2, int n3,
                                   float *sub, int s1, int s2, int s3, int f1, int f2, int f3,
                                   cudaStream_t st) {
-  window_extract_kernel<<<rows_grid(s1, (long long)s2 * s3), 256, 0, st>>>(img, mute, n1, n2, n3, sub,
-                                                                           s1, s2, s3, f1, f2, f3);
+  if (n1 % 4 == 0 && s1 % 4 == 0 && f1 % 4 == 0 && al16(img) && al16(sub) && (!mute || al16(mute))) {
+    const RowsLaunch L = rows_launch4(s1 / 4, (long long)s2 * s3);
+    window_extract4_kernel<<<L.grid, L.block, 0, st>>>(img, mute, n1, n2, n3, sub, s1, s2, s3, f1, f2,
+                                                       f3);
+  } else {
+    window_extract_kernel<<<rows_grid(s1, (long long)s2 * s3), 256, 0, st>>>(img, mute, n1, n2, n3, sub,
+                                                                             s1, s2, s3, f1, f2, f3);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_tmute(const float *in, float *out, int add, float t0, float vmute, int n1,
                          float o1, float d1, int n2, float o2, float d2, long long nrep,
                          cudaStream_t st) {
-  tmute_kernel<<<rows_grid(n1, (long long)n2 * nrep), 256, 0, st>>>(in, out, add, t0, vmute, n1, o1,
-                                                                    d1, n2, o2, d2, nrep);
+  if (n1 % 4 == 0 && al16(in) && al16(out)) {
+    const RowsLaunch L = rows_launch4(n1 / 4, (long long)n2 * nrep);
+    tmute4_kernel<<<L.grid, L.block, 0, st>>>(in, out, add, t0, vmute, n1, o1, d1, n2, o2, d2, nrep);
+  } else {
+    tmute_kernel<<<rows_grid(n1, (long long)n2 * nrep), 256, 0, st>>>(in, out, add, t0, vmute, n1, o1,
+                                                                      d1, n2, o2, d2, nrep);
+  }
   return cudaGetLastError();
 }
 

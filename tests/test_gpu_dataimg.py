@@ -63,6 +63,25 @@ def test_window_add_and_extract_bit_exact(gf, f):
     assert np.array_equal(_bits(out1.cpu().numpy()), _bits(O.extract_sub(want, None, sub.shape, f)))
 
 
+@pytest.mark.parametrize("f", [(4, -1, 2), (-4, 3, -1), (12, 0, 0), (-8, 0, 0)])
+def test_window_add_and_extract_aligned_bit_exact(gf, f):
+    """rows of 16 and 8 floats at offsets that are multiples of 4: the
+    16-byte path, windows inside, straddling and outside along x"""
+    rng = np.random.default_rng(300 + 7 * f[0] + f[1])
+    img = rng.standard_normal((6, 7, 16)).astype(np.float32)
+    sub = rng.standard_normal((4, 5, 8)).astype(np.float32)
+    mute = rng.random((6, 7, 16)).astype(np.float32)
+    ti, ts, tm = _dev(img), _dev(sub), _dev(mute)
+    out = torch.full((4, 5, 8), 7.0, device="cuda")
+    torch.cuda.synchronize()
+    gf.image_add_window(ti.data_ptr(), (16, 7, 6), f, ts.data_ptr(), (8, 5, 4))
+    gf.image_extract_window(ti.data_ptr(), tm.data_ptr(), (16, 7, 6), f, out.data_ptr(), (8, 5, 4))
+    gf.synchronize()
+    want = O.add_image(img, sub, f)
+    assert np.array_equal(_bits(ti.cpu().numpy()), _bits(want))
+    assert np.array_equal(_bits(out.cpu().numpy()), _bits(O.extract_sub(want, mute, sub.shape, f)))
+
+
 @pytest.mark.parametrize("adj", [False, True])
 @pytest.mark.parametrize("add", [False, True])
 def test_tmute_bit_exact(gf, adj, add):
