@@ -55,6 +55,16 @@
 #ifndef SEPX_TMEMQ_ADJ
 #define SEPX_TMEMQ_ADJ 0
 #endif
+// the source propagation: z-queue in tensor memory, CTAs per SM, ring depth
+#ifndef SEPX_TMEMQ_SP
+#define SEPX_TMEMQ_SP 0
+#endif
+#ifndef SEPX_SP_MINB
+#define SEPX_SP_MINB 4
+#endif
+#ifndef SEPX_SP_STAGES
+#define SEPX_SP_STAGES 4
+#endif
 // the linearised forward: z-queues in tensor memory, CTAs per SM, ring depth
 // (tensor memory frees the registers for 3 CTAs per SM: the forward pass of
 // the linearised pair on 256^3 x 1500 steps 0.393 -> 0.386 s)
@@ -120,10 +130,10 @@ struct Mode {
   // z-4 .. z+3 of every step are 32 consecutive columns); the z+4 feed is
   // read from shared memory and written to both copies of its slot
   static constexpr bool TQ = (SEPX_TMEMQ && MODE == kBornFwd) || (SEPX_TMEMQ_ADJ && MODE == kRtmAdj) ||
-                              (SEPX_TMEMQ_LIN && MODE == kLinFwd);
+                              (SEPX_TMEMQ_LIN && MODE == kLinFwd) || (SEPX_TMEMQ_SP && MODE == kSrcProp);
   static constexpr uint32_t TQ_COLS = NF == 2 ? 128u : 64u;
   // resident blocks per SM the register budget is sized for
-  static constexpr int MINB = (MODE == kSrcProp)  ? 4
+  static constexpr int MINB = (MODE == kSrcProp)  ? SEPX_SP_MINB
                               : (MODE == kBornFwd) ? SEPX_FWD_MINB
                               : (MODE == kRtmAdj)  ? SEPX_ADJ_MINB
                               : (MODE == kLinFwd)  ? SEPX_LINFWD_MINB
@@ -843,7 +853,7 @@ cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st) {
   if (wx <= 0 || wy <= 0 || wz <= 0) return cudaSuccess;
   dim3 grid((wx + kTX - 1) / kTX, (wy + kTY - 1) / kTY, (wz + g.zchunk - 1) / g.zchunk);
   switch (mode) {
-    case kSrcProp: return launch_mode<kSrcProp, 4>(P, grid, st);
+    case kSrcProp: return launch_mode<kSrcProp, SEPX_SP_STAGES>(P, grid, st);
     case kBornFwd: return launch_mode<kBornFwd, SEPX_FWD_STAGES>(P, grid, st);
     case kRtmAdj: return launch_mode<kRtmAdj, SEPX_ADJ_STAGES>(P, grid, st);
     case kRtmAdj1: return launch_mode<kRtmAdj1, 3>(P, grid, st);
@@ -950,7 +960,7 @@ int prop_batch_occupancy(int mode, int stages) {
 
 size_t prop_smem_bytes(int mode) {
   switch (mode) {
-    case kSrcProp: return smem_bytes_of<kSrcProp, 4>();
+    case kSrcProp: return smem_bytes_of<kSrcProp, SEPX_SP_STAGES>();
     case kBornFwd: return smem_bytes_of<kBornFwd, SEPX_FWD_STAGES>();
     case kRtmAdj: return smem_bytes_of<kRtmAdj, SEPX_ADJ_STAGES>();
     case kRtmAdj1: return smem_bytes_of<kRtmAdj1, 3>();
