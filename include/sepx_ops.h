@@ -327,7 +327,7 @@ class image_rtm_3d {
   image_rtm_3d(const image_rtm_3d &) = delete;
   void set_mute(const hypercube_float &m);          // copies m (same shape)
   void add_image(const hypercube_float *img);       // image_rtm_3d.cpp:24-49
-  hypercube_float *extract_sub(axis a1, axis a2, axis a3) const;   // :52-90
+  hypercube_float *extract_sub(axis a1, axis a2, axis a3) const;   // :52-90, caller owns it
   void write_volume();                              // image *= mute (:92-104)
   axis get_axis(int i) const { return image->get_axis(i); }
   hypercube_float *image = nullptr, *mute = nullptr;

@@ -678,6 +678,8 @@ int sepx_lsrtm(sepx_op_handle h, const float *data, int niter, float *model, dou
                double *seconds, sepx_direction_fn dir, void *dir_ctx, double fallback_ratio,
                int *fallback_iter) {
   try {
+    if (!h || !data || !model) return sepx::set_error("lsrtm: NULL argument");
+    if (niter < 0) return sepx::set_error("lsrtm: niter %d < 0", niter);
     auto *b = static_cast<op_box *>(h);
     b->data->upload(data);
     cgstep st;
@@ -707,6 +709,8 @@ int sepx_lsrtm_ex(sepx_op_handle h, const float *data, int niter, const sepx_lsr
                   float *model, double *resid, double *seconds, int *used_dir, int *iters_done) {
   try {
     if (!opts) return sepx::set_error("lsrtm_ex: opts is NULL");
+    if (!h || !data || !model) return sepx::set_error("lsrtm_ex: NULL argument");
+    if (niter < 0) return sepx::set_error("lsrtm_ex: niter %d < 0", niter);
     if (opts->policy != SEPX_DIR_FALLBACK && opts->policy != SEPX_DIR_ADAPTIVE)
       return sepx::set_error("lsrtm_ex: unknown direction policy %d", opts->policy);
     auto *b = static_cast<op_box *>(h);
