@@ -293,7 +293,7 @@ struct HaloArgs {
 __host__ __device__ constexpr int halo_groups(int cin) { return ((cin / 8) + 1) & ~1; }
 
 __host__ __device__ constexpr size_t halo_smem_bytes(int cin, uint32_t wbytes, int nbuf) {
-  return (size_t)wbytes + (size_t)nbuf * (size_t)halo_groups(cin) * kHaloGS + 128 + 128;
+  return (size_t)wbytes + (size_t)nbuf * (size_t)halo_groups(cin) * kHaloGS + 256 + 128;
 }
 
 // Warp roles: warp 4 (lane 0) loads the weights and the halos and issues the
@@ -304,6 +304,7 @@ __host__ __device__ constexpr size_t halo_smem_bytes(int cin, uint32_t wbytes, i
 // halo buffer b are done (tcgen05.commit), acc[a] accumulator a complete
 // (commit), afree[a] accumulator a read by the 4 epilogue warps, wbar weights.
 constexpr int kHaloThreads = 160;
+constexpr int kMaxPairs = 8;   // channel-group pairs of one halo (up to 128 channels)
 
 __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_constant__ CUtensorMap tmx,
                                                                  const __nv_bfloat16 *__restrict__ wp,
@@ -318,7 +319,10 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
   const uint32_t hbytes = (uint32_t)ngh * kHaloGS;
   unsigned long long *bar = reinterpret_cast<unsigned long long *>(halo + a.nbuf * hbytes);
   unsigned long long *full = bar, *hfree = bar + 2, *accb = bar + 4, *afree = bar + 6, *wbar = bar + 8;
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 9);
+  // one halo buffer: per pair of channel groups, loaded (pfull) and read by
+  // its MMAs (pfree), so the next tile's halo streams in pair by pair
+  unsigned long long *pfull = bar + 9, *pfree = bar + 9 + kMaxPairs;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 9 + 2 * kMaxPairs);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t acols = a.np <= 32 ? 32 : (a.np <= 64 ? 64 : 128);   // per accumulator
@@ -336,6 +340,10 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
       mbar_init(smem_u32(&hfree[i]), 1);
       mbar_init(smem_u32(&accb[i]), 1);
       mbar_init(smem_u32(&afree[i]), 4);
+    }
+    for (int i = 0; i < kMaxPairs; i++) {
+      mbar_init(smem_u32(&pfull[i]), 1);
+      mbar_init(smem_u32(&pfree[i]), 1);
     }
     mbar_init(smem_u32(wbar), 1);
     *abort_flag = 0;
@@ -378,6 +386,74 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
       prefetch_tmap(&tmx);
       mbar_arrive_expect_tx(smem_u32(wbar), a.wbytes);
       bulk_load(smem_u32(wsm), wp, a.wbytes, smem_u32(wbar));
+      if (a.nbuf == 1) {
+        // ---- one buffer, pipelined by channel-group pair: pair j of tile k
+        // is read by its 27 taps' MMAs, after which pair j of tile k+1 loads
+        // while the MMAs of pair j+1 run (pair-major accumulation order)
+        const int npair = ngh / 2;
+        const uint32_t h0 = smem_u32(halo), w0 = smem_u32(wsm);
+        auto issue_pair = [&](int k, int j) {
+          int n, z, y0, x0;
+          tile_pos(k, n, z, y0, x0);
+          const uint32_t fb = smem_u32(&pfull[j]);
+          mbar_arrive_expect_tx(fb, 2u * (kHaloX * kHaloY * kHaloZ * 16));
+          for (int e = 0; e < 2; e++)
+            tma_load_5d(h0 + (2 * j + e) * kHaloGS, &tmx, 8 * (2 * j + e), x0 - 1, y0 - 1, z - 1, n, fb);
+        };
+        int pi[kMaxPairs], pu[kMaxPairs];   // loads issued / consumed per pair
+        for (int j = 0; j < npair; j++) {
+          issue_pair(0, j);
+          pi[j] = 1;
+          pu[j] = 0;
+        }
+        bool ok = mbar_wait_bounded(smem_u32(wbar), 0, a.err, kErrFullWait);
+        uint32_t last_bar = 0, last_par = 0;   // the latest commit
+        for (int k = 0; ok && k < ntile; k++) {
+          if (*abort_flag) { ok = false; break; }
+          const int ab = k & 1;
+          if (k >= 2 && !mbar_wait_bounded(smem_u32(&afree[ab]), ((k - 2) >> 1) & 1, a.err, kErrMmaWait)) { ok = false; break; }
+          const uint32_t d = tmem + ab * acols;
+          bool first = true;
+          for (int j = 0; ok && j < npair; j++) {
+            if (!mbar_wait_bounded(smem_u32(&pfull[j]), (uint32_t)(k & 1), a.err, kErrFullWait)) { ok = false; break; }
+            pu[j]++;
+            tc::fence_after_sync();
+            for (int tp = 0; tp < 27; tp++) {
+              const int q = (tp * 57) >> 9, r = tp - 9 * q, q3 = (r * 11) >> 5;
+              const uint32_t tap_off = (uint32_t)(((q * kHaloY + q3) * kHaloX + (r - 3 * q3)) * 16);
+              const uint64_t ad = tc::smem_desc(h0 + 2 * j * kHaloGS + tap_off, kHaloGS, kHaloX * 16);
+              const uint64_t bd =
+                  tc::smem_desc(w0 + (uint32_t)((tp * ngc + 2 * j) * ngn * 128), ngn * 128, 128);
+              tc::mma_bf16(d, ad, bd, idesc, first ? 0u : 1u);
+              first = false;
+            }
+            tc::mma_commit(smem_u32(&pfree[j]));
+            last_bar = smem_u32(&pfree[j]);
+            last_par = (uint32_t)(k & 1);
+            // the previous pair's MMAs are queued ahead of these: refill it
+            if (j >= 1 && k + 1 < ntile) {
+              if (!mbar_wait_bounded(smem_u32(&pfree[j - 1]), (uint32_t)(k & 1), a.err, kErrMmaWait)) { ok = false; break; }
+              issue_pair(k + 1, j - 1);
+              pi[j - 1]++;
+            }
+          }
+          if (!ok) break;
+          tc::mma_commit(smem_u32(&accb[ab]));
+          last_bar = smem_u32(&accb[ab]);
+          last_par = (uint32_t)((k >> 1) & 1);
+          if (k + 1 < ntile) {
+            if (!mbar_wait_bounded(smem_u32(&pfree[npair - 1]), (uint32_t)(k & 1), a.err, kErrMmaWait)) { ok = false; break; }
+            issue_pair(k + 1, npair - 1);
+            pi[npair - 1]++;
+          }
+        }
+        if (!ok) *abort_flag = 1;
+        // never leave with a copy or an MMA in flight
+        for (int j = 0; j < npair; j++)
+          for (int i = pu[j]; i < pi[j]; i++)
+            mbar_wait_bounded(smem_u32(&pfull[j]), (uint32_t)(i & 1), a.err, kErrDrainWait);
+        if (last_bar) mbar_wait_bounded(last_bar, last_par, a.err, kErrDrainWait);
+      } else {
       int issued = 0;
       for (; issued < a.nbuf && issued < ntile; issued++) issue_halo(issued);
       bool ok = mbar_wait_bounded(smem_u32(wbar), 0, a.err, kErrFullWait);
@@ -421,6 +497,7 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
       for (int i = k; i < issued; i++) mbar_wait_bounded(smem_u32(&full[hbuf(i)]), hpar(i), a.err, kErrDrainWait);
       // and for the MMAs issued (the last commit covers all of them)
       if (k > 0) mbar_wait_bounded(smem_u32(&hfree[hbuf(k - 1)]), hpar(k - 1), a.err, kErrDrainWait);
+      }
     }
   } else {
     // ---------------- epilogue warps 0-3 ----------------
@@ -941,8 +1018,11 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
     const size_t per = ((halo_smem_bytes(cin, wbytes, nbuf) + 127) / 128) * 128 + g_smem_reserved;
     return (int)(g_smem_per_sm / per);
   };
+  // two or more channel-group pairs: one buffer pipelined pair by pair;
+  // a single pair: two buffers where they still leave two CTAs per SM
   const bool two_fit = halo_smem_bytes(cin, wbytes, 2) <= kHaloMaxSmem;
-  a.nbuf = (two_fit && (fit(2) >= 2 || fit(1) < 2)) ? 2 : 1;
+  if (halo_groups(cin) >= 4) a.nbuf = 1;
+  else a.nbuf = (two_fit && (fit(2) >= 2 || fit(1) < 2)) ? 2 : 1;
   int per_sm = fit(a.nbuf);
   if (per_sm < 1) return set_error("unet conv: the halo kernel does not fit an SM");
   if (per_sm > 8) per_sm = 8;
@@ -1011,7 +1091,7 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
   const long long V = (long long)nb * D * H * W;
   if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
     return set_error("unet conv: volume too large (%lld voxels)", V);
-  if (ntap == 27 && H >= kTileY && W >= kTileX && g_halo_enabled) {
+  if (ntap == 27 && H >= kTileY && W >= kTileX && halo_groups(cin) / 2 <= kMaxPairs && g_halo_enabled) {
     // packed weights of the 27 taps, plus one K group for an odd group count
     // (the packing pads with zeros up to a multiple of 8 groups, and 27 * an
     // odd count is never one)
