@@ -63,6 +63,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: the warp may sleep in hardware until
+// the phase completes or the hint (ns) elapses, instead of spinning
+#ifndef SEPX_WAIT_HINT_NS
+#define SEPX_WAIT_HINT_NS 20000
+#endif
+__device__ __forceinline__ bool mbar_try_wait_hint(uint32_t addr, uint32_t parity) {
+#if SEPX_WAIT_HINT_NS > 0
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity), "n"(SEPX_WAIT_HINT_NS)
+      : "memory");
+  return ok != 0;
+#else
+  return mbar_try_wait(addr, parity);
+#endif
+}
+
 // Wait for the phase with the given parity to complete.  Returns false (and
 // records `code`) when the budget runs out.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity, int *err,
@@ -70,7 +91,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity
   if (mbar_try_wait(addr, parity)) return true;
   const unsigned long long t0 = globaltimer_ns();
   while (true) {
-    if (mbar_try_wait(addr, parity)) return true;
+    if (mbar_try_wait_hint(addr, parity)) return true;
     if (globaltimer_ns() - t0 > kWaitBudgetNs) {
       if (err) atomicCAS(err, 0, code);
       return false;
