@@ -207,11 +207,30 @@ __device__ __forceinline__ float damp_k(float v, float t) {
   return v;
 }
 
+// z-pair sums of a queue (plane z-4+j in qz[j]): zs[k-1] = qz[4+k] + qz[4-k]
+__device__ __forceinline__ void zpairs(const float4 (&qz)[9], float4 (&zs)[4]) {
+#pragma unroll
+  for (int k = 1; k <= 4; k++)
+    zs[k - 1] = make_float4(__fadd_rn(qz[4 + k].x, qz[4 - k].x), __fadd_rn(qz[4 + k].y, qz[4 - k].y),
+                            __fadd_rn(qz[4 + k].z, qz[4 - k].z), __fadd_rn(qz[4 + k].w, qz[4 - k].w));
+}
+
+// z-pair k of column c: from the 9-plane queue, summed where it is used, or
+// from the pair sums
+__device__ __forceinline__ float zterm(const float4 (&qz)[9], int k, int c) {
+  return __fadd_rn(comp(qz[4 + k], c), comp(qz[4 - k], c));
+}
+__device__ __forceinline__ float zterm(const float4 (&zs)[4], int k, int c) {
+  return comp(zs[k - 1], c);
+}
+
 // Laplacian part of wave_kernel (vel outside): s = c0 p + sum_k pairs.
-// xw: x-4 .. x+7 of the row, ym/yp: rows y-k / y+k, qz: z-queue (plane z-4+j).
+// xw: x-4 .. x+7 of the row, ym/yp: rows y-k / y+k, zq: the z-queue (plane
+// z-4+j in zq[j]) or its pair sums.
+template <int NZ>
 __device__ __forceinline__ void lap_plain(const float *coef, const float (&xw)[12],
                                           const float4 (&ym)[4], const float4 (&yp)[4],
-                                          const float4 (&qz)[9], float (&s)[4]) {
+                                          const float4 (&zq)[NZ], float (&s)[4]) {
 #pragma unroll
   for (int c = 0; c < 4; c++) {
     float p = xw[4 + c];
@@ -220,18 +239,19 @@ __device__ __forceinline__ void lap_plain(const float *coef, const float (&xw)[1
     for (int k = 1; k <= 4; k++) {
       acc = __fmaf_rn(coef[3 * k - 2], __fadd_rn(xw[4 + c + k], xw[4 + c - k]), acc);
       acc = __fmaf_rn(coef[3 * k - 1], __fadd_rn(comp(yp[k - 1], c), comp(ym[k - 1], c)), acc);
-      acc = __fmaf_rn(coef[3 * k], __fadd_rn(comp(qz[4 + k], c), comp(qz[4 - k], c)), acc);
+      acc = __fmaf_rn(coef[3 * k], zterm(zq, k, c), acc);
     }
     s[c] = acc;
   }
 }
 
 // Laplacian of (v p), wave_kernel_adj (vel inside): centre (c0 p) v, pairs of
-// rounded products; qz holds the products p v along z.
+// rounded products; zq: z-queue of the products p v, or its pair sums.
+template <int NZ>
 __device__ __forceinline__ void lap_velin(const float *coef, const float (&xw)[12],
                                           const float (&vw)[12], const float4 (&ym)[4],
                                           const float4 (&yp)[4], const float4 (&vym)[4],
-                                          const float4 (&vyp)[4], const float4 (&qz)[9],
+                                          const float4 (&vyp)[4], const float4 (&zq)[NZ],
                                           float (&s)[4]) {
 #pragma unroll
   for (int c = 0; c < 4; c++) {
@@ -244,7 +264,7 @@ __device__ __forceinline__ void lap_velin(const float *coef, const float (&xw)[1
       float py = __fadd_rn(__fmul_rn(comp(yp[k - 1], c), comp(vyp[k - 1], c)),
                            __fmul_rn(comp(ym[k - 1], c), comp(vym[k - 1], c)));
       acc = __fmaf_rn(coef[3 * k - 1], py, acc);
-      acc = __fmaf_rn(coef[3 * k], __fadd_rn(comp(qz[4 + k], c), comp(qz[4 - k], c)), acc);
+      acc = __fmaf_rn(coef[3 * k], zterm(zq, k, c), acc);
     }
     s[c] = acc;
   }
@@ -402,17 +422,31 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
     for (int i = 0; i < niter; i++) {
       const int s = i % STAGES;
       const bool ok = mbar_wait_bounded(smem_u32(&bar_full[s]), (i / STAGES) & 1, P.err, kErrFullWait);
-      if (M::TQ) {
+      float4 zs[NF][4];   // M::TQ: z-pair sums of each field's queue
+      if constexpr (M::TQ) {
         // tensor-memory operations are warp-wide: leave the loop together
         if (!__all_sync(0xffffffffu, ok)) break;
-        // the previous plane's feed is in place (its stores were waited for)
-        if (NF == 2)
-          tc::tmem_ld32_q8_pair(tq + 4 * (i & 7), tq + 64 + 4 * (i & 7), q[0], q[NF - 1]);
-        else
-          tc::tmem_ld32_q8(tq + 4 * (i & 7), q[0]);
-        q[0][8] = q[NF - 1][8] = make_float4(0.f, 0.f, 0.f, 0.f);
-      } else if (!ok) {
-        break;
+        // field by field: its 8 planes z-4 .. z+3 (the previous plane's feed
+        // is in place: its stores were waited for) and the z+4 feed, folded
+        // into the four pair sums at once; then the feed replaces plane z-4
+        // (slot i & 7 and its copy).  One field's ring at a time is held in
+        // registers.
+        const float *sf = smem + s * M::STAGE;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          float4 qf[9];
+          tc::tmem_ld32_q8(tq + f * 64 + 4 * (i & 7), qf);
+          float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (active) {
+            p = lds4(sf + M::FEED + f * kCenterFloats + coff);
+            if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, lds4(sf + M::FEEDV + coff));
+          }
+          qf[8] = p;
+          zpairs(qf, zs[f]);
+          tc::tmem_st4x2_sync(tq + f * 64 + 4 * (i & 7), tq + f * 64 + 4 * ((i & 7) + 8), p);
+        }
+      } else {
+        if (!ok) break;
       }
       const float *st = smem + s * M::STAGE;
       const int z = za + i;
@@ -426,11 +460,13 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
       float vwc[4];
       if (active) {
         // z-queue feed: plane z+4
+        if constexpr (!M::TQ) {
 #pragma unroll
-        for (int f = 0; f < NF; f++) {
-          float4 p = lds4(st + M::FEED + f * kCenterFloats + coff);
-          if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, lds4(st + M::FEEDV + coff));
-          q[f][8] = p;
+          for (int f = 0; f < NF; f++) {
+            float4 p = lds4(st + M::FEED + f * kCenterFloats + coff);
+            if (f == 0 && M::F0_VEL_INSIDE) p = mul4(p, lds4(st + M::FEEDV + coff));
+            q[f][8] = p;
+          }
         }
         float vw[12];
         float4 vym[4], vyp[4];
@@ -448,12 +484,18 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
           load_window(st + M::HALO + f * kHaloFloats + hoff, xw, ym, yp);
           float sl[4];
           if (f == 0 && M::F0_VEL_INSIDE) {
-            lap_velin(P.coef, xw, vw, ym, yp, vym, vyp, q[f], sl);
+            if constexpr (M::TQ)
+              lap_velin(P.coef, xw, vw, ym, yp, vym, vyp, zs[f], sl);
+            else
+              lap_velin(P.coef, xw, vw, ym, yp, vym, vyp, q[f], sl);
 #pragma unroll
             for (int c = 0; c < 4; c++)
               res[f][c] = M::INC0 ? sl[c] : __fadd_rn(__fadd_rn(sl[c], xw[4 + c]), xw[4 + c]);
           } else {
-            lap_plain(P.coef, xw, ym, yp, q[f], sl);
+            if constexpr (M::TQ)
+              lap_plain(P.coef, xw, ym, yp, zs[f], sl);
+            else
+              lap_plain(P.coef, xw, ym, yp, q[f], sl);
 #pragma unroll
             for (int c = 0; c < 4; c++)
               res[f][c] = (f == 0 && M::INC0)
@@ -677,13 +719,6 @@ __device__ __forceinline__ void run_tile(const PropParams &P, const PropParams &
           for (int f = 0; f < NF; f++)
 #pragma unroll
             for (int j = 0; j < 8; j++) q[f][j] = q[f][j + 1];
-        }
-      }
-      if (M::TQ) {
-        // the z+4 plane replaces z-4 (slot i & 7 and its copy)
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-          tc::tmem_st4x2_sync(tq + f * 64 + 4 * (i & 7), tq + f * 64 + 4 * ((i & 7) + 8), q[f][8]);
         }
       }
     }
