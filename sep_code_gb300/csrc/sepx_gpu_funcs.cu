@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <memory>
 #include <cmath>
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -139,6 +140,16 @@ int fail(const char *fmt, ...) {
     int r_ = (x);         \
     if (r_) return r_;    \
   } while (0)
+
+// a buffer the call reads or writes: NULL is reported, never dereferenced
+int need_buf(const void *p, const char *what) {
+  return p ? 0 : fail("%s: NULL buffer", what);
+}
+// n elements at p (host or device): n >= 0, and p given when n > 0
+int need_span(const void *p, long long n, const char *what) {
+  if (n < 0) return fail("%s: negative length %lld", what, n);
+  return n > 0 ? need_buf(p, what) : 0;
+}
 
 template <class T>
 int ensure(T **p, size_t *cap, size_t n) {
@@ -725,6 +736,8 @@ static int upload_sinc(int nsinc, int n, float **tables, float **dst, int *nrows
   RET(need_device());
   if (nsinc < 8) return fail("sinc tables need at least 8 taps (got %d)", nsinc);
   if (n < 1) return fail("empty sinc table");
+  RET(need_buf(tables, "sinc tables"));
+  for (int i = 0; i < n; i++) RET(need_buf(tables[i], "sinc table row"));
   std::vector<float> flat((size_t)nsinc * n);
   for (int i = 0; i < n; i++) memcpy(&flat[(size_t)i * nsinc], tables[i], sizeof(float) * nsinc);
   cudaFree(*dst);
@@ -745,8 +758,10 @@ int sepx_transfer_sinc_table_d(int nsinc, int nd, float **tables) {
 }
 
 int sepx_transfer_source_func(int npts, int nt, const int *locs, const float *vals) {
-  RET(need_grid());
   if (npts < 0 || nt < 1) return fail("invalid source shape %d x %d", npts, nt);
+  RET(need_span(locs, npts, "transfer_source_func locs"));
+  RET(need_span(vals, npts, "transfer_source_func vals"));
+  RET(need_grid());
   G.src_loc.assign(locs, locs + npts);
   G.npts_s = npts;
   G.src_ntrace = nt;
@@ -760,9 +775,12 @@ int sepx_transfer_source_func(int npts, int nt, const int *locs, const float *va
 }
 
 int sepx_transfer_receiver_func(int nx, int ny, int nt, const int *locs, const float *vals) {
-  RET(need_grid());
   if (nx < 0 || ny < 0 || nt < 1) return fail("invalid receiver shape %d x %d x %d", nx, ny, nt);
+  if ((long long)nx * ny > INT_MAX) return fail("too many receivers: %d x %d", nx, ny);
   const int nrec = nx * ny;
+  RET(need_span(locs, nrec, "transfer_receiver_func locs"));
+  RET(need_span(vals, nrec, "transfer_receiver_func vals"));
+  RET(need_grid());
   G.rec_nx = nx;
   G.rec_ny = ny;
   G.rec_ntrace = nt;
@@ -777,9 +795,11 @@ int sepx_transfer_receiver_func(int nx, int ny, int nt, const int *locs, const f
 }
 
 int sepx_set_receivers(int nx, int ny, int nt, const int *locs) {
-  RET(need_grid());
   if (nx < 0 || ny < 0 || nt < 1) return fail("invalid receiver shape %d x %d x %d", nx, ny, nt);
+  if ((long long)nx * ny > INT_MAX) return fail("too many receivers: %d x %d", nx, ny);
   const int nrec = nx * ny;
+  RET(need_span(locs, nrec, "set_receivers locs"));
+  RET(need_grid());
   G.rec_nx = nx;
   G.rec_ny = ny;
   G.rec_ntrace = nt;
@@ -793,6 +813,7 @@ int sepx_set_receivers(int nx, int ny, int nt, const int *locs) {
 }
 
 int sepx_transfer_vel_func1(int nx, int ny, int nz, const float *vel) {
+  RET(need_buf(vel, "transfer_vel_func1 vel"));
   RET(need_grid());
   RET(check_dims(nx, ny, nz));
   RET(h2d_volume(G.vel, vel));
@@ -812,6 +833,10 @@ int sepx_transfer_vel_func2(int nx, int ny, int nz, const float *vel) {
 int sepx_source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0, float *p1, int jt,
                      int npts, int nt) {
   (void)damp;
+  if (get_last) {
+    RET(need_buf(p0, "source_prop p0"));
+    RET(need_buf(p1, "source_prop p1"));
+  }
   RET(need_grid());
   RET(check_dims(n1, n2, n3));
   RET(loop_source_prop(jt, npts, nt));
@@ -825,6 +850,8 @@ int sepx_source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0
 
 int sepx_rtm_forward(int n1, int n2, int n3, int jt, const float *img, float *dat, int npts_src,
                      int nt, int nt_big, int nx, int ny) {
+  RET(need_buf(img, "rtm_forward img"));
+  RET(need_span(dat, (long long)nx * ny, "rtm_forward dat"));
   RET(need_grid());
   RET(check_dims(n1, n2, n3));
   if (nx != G.rec_nx || ny != G.rec_ny)
@@ -840,6 +867,9 @@ int sepx_rtm_forward(int n1, int n2, int n3, int jt, const float *img, float *da
 
 int sepx_rtm_adjoint(int n1, int n2, int n3, int jt, const float *p0_s, const float *p1_s,
                      float *img, int npts, int nt) {
+  RET(need_buf(p0_s, "rtm_adjoint p0_s"));
+  RET(need_buf(p1_s, "rtm_adjoint p1_s"));
+  RET(need_buf(img, "rtm_adjoint img"));
   RET(need_grid());
   RET(check_dims(n1, n2, n3));
   RET(h2d_volume(G.F[2], p0_s));
@@ -889,12 +919,14 @@ long long sepx_snapshot_bytes(int nt, int js, int prec) {
 }
 
 int sepx_set_image(const float *img) {
+  RET(need_buf(img, "set_image"));
   RET(need_grid());
   RET(h2d_volume(G.img, img));
   return 0;
 }
 
 int sepx_get_image(float *img) {
+  RET(need_buf(img, "get_image"));
   RET(need_grid());
   RET(d2h_volume(img, G.img));
   CK(cudaStreamSynchronize(G.stream));
@@ -902,6 +934,8 @@ int sepx_get_image(float *img) {
 }
 
 int sepx_set_source_fields(const float *p0, const float *p1) {
+  RET(need_buf(p0, "set_source_fields p0"));
+  RET(need_buf(p1, "set_source_fields p1"));
   RET(need_grid());
   RET(h2d_volume(G.F[2], p0));
   RET(h2d_volume(G.F[3], p1));
@@ -909,6 +943,8 @@ int sepx_set_source_fields(const float *p0, const float *p1) {
 }
 
 int sepx_get_source_fields(float *p0, float *p1) {
+  RET(need_buf(p0, "get_source_fields p0"));
+  RET(need_buf(p1, "get_source_fields p1"));
   RET(need_grid());
   if (!G.sl_valid) return fail("no source wavefields");
   RET(d2h_volume(p0, G.SL[G.sl_p0]));
@@ -920,6 +956,7 @@ int sepx_get_source_fields(float *p0, float *p1) {
 int sepx_set_traces(const float *vals) {
   RET(need_grid());
   const int nrec = G.rec_nx * G.rec_ny;
+  RET(need_span(vals, nrec, "set_traces"));
   if (nrec > 0) RET(traces_h2d(vals, nrec, G.rec_ntrace));
   return 0;
 }
@@ -927,6 +964,7 @@ int sepx_set_traces(const float *vals) {
 int sepx_get_traces(float *vals) {
   RET(need_grid());
   const int nrec = G.rec_nx * G.rec_ny;
+  RET(need_span(vals, nrec, "get_traces"));
   if (nrec > 0) RET(traces_d2h(vals, nrec, G.rec_ntrace));
   CK(cudaStreamSynchronize(G.stream));
   return 0;
@@ -939,8 +977,9 @@ int sepx_zero_traces(void) {
 }
 
 int sepx_dot_f32(const float *a, const float *b, long long n, double *result) {
+  RET(need_buf(result, "sepx_dot_f32 result"));
+  RET(need_span(a, n, "sepx_dot_f32 a"));   // b == NULL: the sum of a
   RET(need_device());
-  if (n < 0 || !result) return fail("sepx_dot_f32: invalid arguments");
   const int np = vec_dot_scratch_doubles();
   RET(ensure(&G.d_dot, &G.dot_cap, (size_t)np + 1));
   CKL(vec_dot(a, b, n, G.d_dot, G.d_dot + np, G.stream));
@@ -951,6 +990,7 @@ int sepx_dot_f32(const float *a, const float *b, long long n, double *result) {
 
 // ------------------------------------------------------------ operator glue
 int sepx_op_image_to_padded(const float *model, int m1, int m2, int m3, int f1, int f2, int f3) {
+  RET(need_buf(model, "op_image_to_padded model"));
   RET(need_grid());
   CKL(launch_img_from_model(model, m1, m2, m3, f1, f2, f3, G.img.origin, G.n1, G.n2, G.n3, G.pitch,
                             G.stream));
@@ -958,6 +998,7 @@ int sepx_op_image_to_padded(const float *model, int m1, int m2, int m3, int f1, 
 }
 
 int sepx_op_padded_to_image(float *model, int m1, int m2, int m3, int f1, int f2, int f3) {
+  RET(need_buf(model, "op_padded_to_image model"));
   RET(need_grid());
   CKL(launch_model_from_img(model, m1, m2, m3, f1, f2, f3, G.img.origin, G.n1, G.n2, G.n3, G.pitch,
                             G.stream));
@@ -965,6 +1006,7 @@ int sepx_op_padded_to_image(float *model, int m1, int m2, int m3, int f1, int f2
 }
 
 int sepx_op_traces_to_data(float *data, int nt, float dt) {
+  RET(need_buf(data, "op_traces_to_data data"));
   RET(need_grid());
   const int nrec = G.rec_nx * G.rec_ny;
   if (nt < 2 || nt + 4 > G.rec_ntrace) return fail("data length %d does not fit traces of %d", nt, G.rec_ntrace);
@@ -973,6 +1015,7 @@ int sepx_op_traces_to_data(float *data, int nt, float dt) {
 }
 
 int sepx_op_data_to_traces(const float *data, int nt, float dt) {
+  RET(need_buf(data, "op_data_to_traces data"));
   RET(need_grid());
   const int nrec = G.rec_nx * G.rec_ny;
   if (nt < 2 || nt + 4 > G.rec_ntrace) return fail("data length %d does not fit traces of %d", nt, G.rec_ntrace);
@@ -1019,6 +1062,8 @@ int sepx_tmute(int adj, int add, float t0, float vmute, int n1, float o1, float 
 
 // ------------------------------------------------------------ device vectors (BLAS-1)
 int sepx_vec_alloc(float **p, long long n) {
+  RET(need_buf(p, "vec_alloc"));
+  if (n < 0) return fail("vec_alloc: negative length %lld", n);
   RET(need_device());
   CK(cudaMalloc((void **)p, sizeof(float) * (size_t)std::max(n, 1LL)));
   return 0;
@@ -1028,53 +1073,71 @@ int sepx_vec_free(float *p) {
   return 0;
 }
 int sepx_vec_upload(float *d, const float *h, long long n) {
+  RET(need_span(d, n, "vec_upload d"));
+  RET(need_span(h, n, "vec_upload h"));
   RET(need_device());
   CK(cudaMemcpyAsync(d, h, sizeof(float) * n, cudaMemcpyHostToDevice, G.stream));
   CK(cudaStreamSynchronize(G.stream));
   return 0;
 }
 int sepx_vec_download(float *h, const float *d, long long n) {
+  RET(need_span(h, n, "vec_download h"));
+  RET(need_span(d, n, "vec_download d"));
   RET(need_device());
   CK(cudaMemcpyAsync(h, d, sizeof(float) * n, cudaMemcpyDeviceToHost, G.stream));
   CK(cudaStreamSynchronize(G.stream));
   return 0;
 }
 int sepx_vec_copy(float *dst, const float *src, long long n) {
+  RET(need_span(dst, n, "vec_copy dst"));
+  RET(need_span(src, n, "vec_copy src"));
   RET(need_device());
   CK(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, G.stream));
   return 0;
 }
 int sepx_vec_fill(float *x, long long n, float v) {
+  RET(need_span(x, n, "vec_fill x"));
   RET(need_device());
   CKL(vec_fill(x, n, v, G.stream));
   return 0;
 }
 int sepx_vec_scale(float *y, long long n, double a) {
+  RET(need_span(y, n, "vec_scale y"));
   RET(need_device());
   CKL(vec_scale(y, n, a, G.stream));
   return 0;
 }
 int sepx_vec_scale_add(float *y, const float *x, long long n, double a, double b) {
+  RET(need_span(y, n, "vec_scale_add y"));
+  RET(need_span(x, n, "vec_scale_add x"));
   RET(need_device());
   CKL(vec_scale_add(y, x, n, a, b, G.stream));
   return 0;
 }
 int sepx_vec_scale_add2(float *y, const float *x1, const float *x2, long long n, double a, double b) {
+  RET(need_span(y, n, "vec_scale_add2 y"));
+  RET(need_span(x1, n, "vec_scale_add2 x1"));
+  RET(need_span(x2, n, "vec_scale_add2 x2"));
   RET(need_device());
   CKL(vec_scale_add2(y, x1, x2, n, a, b, G.stream));
   return 0;
 }
 int sepx_vec_add(float *y, const float *x, long long n) {
+  RET(need_span(y, n, "vec_add y"));
+  RET(need_span(x, n, "vec_add x"));
   RET(need_device());
   CKL(vec_add(y, x, n, G.stream));
   return 0;
 }
 int sepx_vec_mult(float *y, const float *x, long long n) {
+  RET(need_span(y, n, "vec_mult y"));
+  RET(need_span(x, n, "vec_mult x"));
   RET(need_device());
   CKL(vec_mult(y, x, n, G.stream));
   return 0;
 }
 int sepx_vec_random(float *y, long long n, unsigned long long seed) {
+  RET(need_span(y, n, "vec_random y"));
   RET(need_device());
   CKL(vec_random(y, n, seed, G.stream));
   return 0;
