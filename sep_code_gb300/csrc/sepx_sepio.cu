@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cerrno>
+#include <climits>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -126,14 +127,26 @@ int layout_of(const Header &h, Layout *L) {
   for (int a = 0; a < kSepMaxAxes; a++) {
     const std::string s = std::to_string(a + 1);
     const std::string *nv = find(h, "n" + s), *ov = find(h, "o" + s), *dv = find(h, "d" + s);
-    L->n[a] = nv ? atoi(nv->c_str()) : 1;
+    if (nv) {
+      char *end = nullptr;
+      const long long v = strtoll(nv->c_str(), &end, 10);
+      if (end == nv->c_str() || v < 1 || v > INT_MAX)
+        return set_error("sep: %s: n%d=%s", h.path.c_str(), a + 1, nv->c_str());
+      L->n[a] = (int)v;
+    } else {
+      L->n[a] = 1;
+    }
     L->o[a] = ov ? strtof(ov->c_str(), nullptr) : 0.f;
     L->d[a] = dv ? strtof(dv->c_str(), nullptr) : 1.f;
     if (L->n[a] < 1) return set_error("sep: %s: n%d=%d", h.path.c_str(), a + 1, L->n[a]);
     if (nv && L->n[a] > 1) L->ndim = a + 1;
   }
   L->n123 = 1;
-  for (int a = 0; a < kSepMaxAxes; a++) L->n123 *= L->n[a];
+  for (int a = 0; a < kSepMaxAxes; a++) {
+    if (L->n123 > (1LL << 60) / L->n[a])   // n[a] >= 1 here
+      return set_error("sep: %s: the axes hold more than 2^60 elements", h.path.c_str());
+    L->n123 *= L->n[a];
+  }
   const std::string *es = find(h, "esize");
   if (es && atoi(es->c_str()) != 4)
     return set_error("sep: %s: esize=%s (only 4-byte floats are read)", h.path.c_str(), es->c_str());
@@ -282,9 +295,9 @@ int sepx_sep_read(const char *header, long long first, long long count, float *d
   Header h;
   Layout L;
   if (int r = open_layout(header, &h, &L)) return r;
-  if (!dst || first < 0 || count < 0 || first + count > L.n123)
-    return set_error("sep_read: elements [%lld, %lld) outside the %lld of %s", first, first + count,
-                     L.n123, header);
+  if (!dst || first < 0 || count < 0 || first > L.n123 || count > L.n123 - first)
+    return set_error("sep_read: %lld elements from %lld do not lie inside the %lld of %s", count,
+                     first, L.n123, header);
   int rc;
   cudaStream_t st = lib_stream(on_device != 0, &rc);
   if (rc) return rc;

@@ -95,3 +95,9 @@ def test_errors(tmp_path):
         S.read_window(tmp_path / "ok.H", [2, 2], [2, 0], [1, 1])   # 2 + 1 >= 3
     with pytest.raises(SepxError):
         S.read(tmp_path / "ok.H", 4, 3)
+    # axis lengths that are not positive ints, or whose product overflows
+    for text in ("n1=abc in=x.H@\n", "n1=3000000000 in=x.H@\n",
+                 "n1=2000000000 n2=2000000000 n3=2000000000 in=x.H@\n"):
+        bad.write_text(text)
+        with pytest.raises(SepxError):
+            S.info(bad)
