@@ -47,6 +47,7 @@ typedef int (*sepx_direction_fn)(void *ctx, float *g, long long n);
 
 sepx_op_handle sepx_rtm_op_create(const sepx_rtm_problem *p);
 void sepx_rtm_op_destroy(sepx_op_handle op);
+/* element counts of the operator's model and data vectors (-1: NULL op) */
 long long sepx_rtm_op_model_size(sepx_op_handle op);
 long long sepx_rtm_op_data_size(sepx_op_handle op);
 /* host-buffer forward / adjoint (rtm_zero_op::forward / ::adjoint) */

@@ -619,11 +619,15 @@ extern "C" {
 
 sepx_op_handle sepx_rtm_op_create(const sepx_rtm_problem *p) {
   try {
-    auto *b = new op_box;
+    if (!p) {
+      sepx::set_error("rtm_zero_op: problem is NULL");
+      return nullptr;
+    }
+    std::unique_ptr<op_box> b(new op_box);
     b->op.reset(new rtm_zero_op(*p));
     b->model.reset(b->op->new_model());
     b->data.reset(b->op->new_data());
-    return b;
+    return b.release();
   } catch (const std::exception &e) {
     sepx::set_error("rtm_zero_op: %s", e.what());
     return nullptr;
@@ -633,13 +637,18 @@ sepx_op_handle sepx_rtm_op_create(const sepx_rtm_problem *p) {
 void sepx_rtm_op_destroy(sepx_op_handle h) { delete static_cast<op_box *>(h); }
 
 long long sepx_rtm_op_model_size(sepx_op_handle h) {
+  if (!h) return sepx::set_error("model_size: NULL operator");
   return static_cast<op_box *>(h)->model->n123;
 }
 
-long long sepx_rtm_op_data_size(sepx_op_handle h) { return static_cast<op_box *>(h)->data->n123; }
+long long sepx_rtm_op_data_size(sepx_op_handle h) {
+  if (!h) return sepx::set_error("data_size: NULL operator");
+  return static_cast<op_box *>(h)->data->n123;
+}
 
 int sepx_rtm_op_forward(sepx_op_handle h, int add, const float *model, float *data) {
   try {
+    if (!h || !model || !data) return sepx::set_error("forward: NULL argument");
     auto *b = static_cast<op_box *>(h);
     b->model->upload(model);
     if (add) b->data->upload(data);
@@ -653,6 +662,7 @@ int sepx_rtm_op_forward(sepx_op_handle h, int add, const float *model, float *da
 
 int sepx_rtm_op_adjoint(sepx_op_handle h, int add, float *model, const float *data) {
   try {
+    if (!h || !model || !data) return sepx::set_error("adjoint: NULL argument");
     auto *b = static_cast<op_box *>(h);
     b->data->upload(data);
     if (add) b->model->upload(model);
@@ -666,6 +676,7 @@ int sepx_rtm_op_adjoint(sepx_op_handle h, int add, float *model, const float *da
 
 int sepx_rtm_op_dot_test(sepx_op_handle h, unsigned long long seed, double out[4]) {
   try {
+    if (!h || !out) return sepx::set_error("dot_test: NULL argument");
     g_random_seed = seed;
     static_cast<op_box *>(h)->op->dot_test(false, out);
     return 0;
