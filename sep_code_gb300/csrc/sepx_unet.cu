@@ -1050,6 +1050,18 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
 }
 }  // namespace
 
+namespace {
+// a device operand the kernel dereferences: NULL is an error, never a launch
+int need_dev(const void *p, const char *what) {
+  return p ? 0 : sepx::set_error("unet: %s is NULL", what);
+}
+int need_dims(int nb, int D, int H, int W, const char *what) {
+  return (nb >= 1 && D >= 1 && H >= 1 && W >= 1)
+             ? 0
+             : sepx::set_error("unet %s: empty volume %d x %d x %d x %d", what, nb, D, H, W);
+}
+}  // namespace
+
 extern "C" {
 
 int sepx_unet_set_halo(int enable) {
@@ -1066,8 +1078,9 @@ int sepx_unet_packed_elems(int cout, int cin_p, int ntap, int transpose) {
 
 int sepx_unet_pack_weights(const float *w, int cout, int cin_p, int ntap, int transpose, void *out,
                            void *stream) {
+  if (need_dev(w, "pack weights w") || need_dev(out, "pack weights out")) return -1;
   const int nout = transpose ? cin_p : cout, kin = transpose ? ((cout + 7) / 8) * 8 : cin_p;
-  if (nout > kMaxN || cin_p % 8 || (ntap != 1 && ntap != 27))
+  if (cout < 1 || cin_p < 8 || nout > kMaxN || cin_p % 8 || (ntap != 1 && ntap != 27))
     return set_error("unet pack: channels (%d -> %d) unsupported", kin, nout);
   const int np = np_of(nout), kch = (ntap * kin + kKC - 1) / kKC;
   pack_weights_kernel<<<grid_for((long long)kch * kKC * np), 256, 0, (cudaStream_t)stream>>>(
@@ -1079,6 +1092,9 @@ int sepx_unet_pack_weights(const float *w, int cout, int cin_p, int ntap, int tr
 int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
                        int ntap, const void *wpacked, const float *bias, int cout, int relu, void *y,
                        int y_cstride, int y_coff, float *yf, const float *resid, void *stream) {
+  if (need_dev(x, "conv x") || need_dev(wpacked, "conv weights") || need_dims(nb, D, H, W, "conv"))
+    return -1;
+  if (!y && !yf) return set_error("unet conv: no output (y and yf are NULL)");
   if (check_conv_args(cin, x_cstride, x_coff, cout, ntap))
     return set_error("unet conv: bad channel arguments (cin %d cstride %d coff %d cout %d ntap %d)", cin,
                      x_cstride, x_coff, cout, ntap);
@@ -1120,6 +1136,9 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
 int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
                          int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
                          float *dw, void *stream) {
+  if (need_dev(x, "wgrad x") || need_dev(dy, "wgrad dy") || need_dev(dw, "wgrad dw") ||
+      need_dims(nb, D, H, W, "wgrad"))
+    return -1;
   if (check_conv_args(cin, x_cstride, x_coff, cout, ntap) || dy_cstride % 8 || dy_coff % 8 ||
       dy_coff + ((cout + 7) / 8) * 8 > dy_cstride)
     return set_error("unet wgrad: bad channel arguments");
@@ -1153,6 +1172,8 @@ int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D
 
 int sepx_unet_avgpool(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int c,
                       void *y, int y_cstride, int y_coff, void *stream) {
+  if (need_dev(x, "avgpool x") || need_dev(y, "avgpool y") || need_dims(nb, D, H, W, "avgpool"))
+    return -1;
   if (c % 8 || D % 2 || H % 2 || W % 2) return set_error("unet avgpool: bad shape");
   View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
   avgpool_kernel<<<grid_for((long long)nb * D * H * W / 8 * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
@@ -1162,6 +1183,9 @@ int sepx_unet_avgpool(const void *x, int x_cstride, int x_coff, int nb, int D, i
 
 int sepx_unet_avgpool_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
                           int c, void *dx, int dx_cstride, int dx_coff, int accumulate, void *stream) {
+  if (need_dev(dy, "avgpool_bwd dy") || need_dev(dx, "avgpool_bwd dx") ||
+      need_dims(nb, D, H, W, "avgpool_bwd"))
+    return -1;
   if (c % 8 || D % 2 || H % 2 || W % 2) return set_error("unet avgpool_bwd: bad shape");
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
   avgpool_bwd_kernel<<<grid_for((long long)nb * D * H * W * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
@@ -1171,6 +1195,8 @@ int sepx_unet_avgpool_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, i
 
 int sepx_unet_upsample(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int c,
                        void *y, int y_cstride, int y_coff, void *stream) {
+  if (need_dev(x, "upsample x") || need_dev(y, "upsample y") || need_dims(nb, D, H, W, "upsample"))
+    return -1;
   if (c % 8) return set_error("unet upsample: bad shape");
   View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
   upsample_kernel<<<grid_for((long long)nb * D * H * W * 8 * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
@@ -1180,6 +1206,9 @@ int sepx_unet_upsample(const void *x, int x_cstride, int x_coff, int nb, int D, 
 
 int sepx_unet_upsample_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
                            int c, void *dx, int dx_cstride, int dx_coff, void *stream) {
+  if (need_dev(dy, "upsample_bwd dy") || need_dev(dx, "upsample_bwd dx") ||
+      need_dims(nb, D, H, W, "upsample_bwd"))
+    return -1;
   if (c % 8) return set_error("unet upsample_bwd: bad shape");
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
   upsample_bwd_kernel<<<grid_for((long long)nb * D * H * W * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
@@ -1189,7 +1218,9 @@ int sepx_unet_upsample_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, 
 
 int sepx_unet_relu_mask(const void *y, int y_cstride, int y_coff, void *dy, int dy_cstride,
                         int dy_coff, long long V, int c, void *stream) {
-  if (c % 8) return set_error("unet relu_mask: bad shape");
+  if (c % 8 || V < 0) return set_error("unet relu_mask: bad shape");
+  if (V == 0 || c == 0) return 0;
+  if (need_dev(y, "relu_mask y") || need_dev(dy, "relu_mask dy")) return -1;
   View yv{(const __nv_bfloat16 *)y, y_cstride, y_coff};
   relu_mask_kernel<<<grid_for(V * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
       yv, (__nv_bfloat16 *)dy, dy_cstride, dy_coff, V, c);
@@ -1198,7 +1229,9 @@ int sepx_unet_relu_mask(const void *y, int y_cstride, int y_coff, void *dy, int 
 
 int sepx_unet_bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V, int c, float *db,
                         void *stream) {
-  if (c > kMaxN) return set_error("unet bias_grad: too many channels");
+  if (c > kMaxN || c < 0 || V < 0) return set_error("unet bias_grad: bad shape");
+  if (V == 0 || c == 0) return 0;
+  if (need_dev(dy, "bias_grad dy") || need_dev(db, "bias_grad db")) return -1;
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
   bias_grad_kernel<<<grid_for(V * c), 256, 0, (cudaStream_t)stream>>>(dv, V, c, db);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet bias_grad: launch failed");
@@ -1206,6 +1239,9 @@ int sepx_unet_bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V
 
 int sepx_unet_to_bf16(const float *in, long long V, float scale, void *y, int y_cstride, int y_coff,
                       void *stream) {
+  if (V < 0) return set_error("unet to_bf16: negative length");
+  if (V == 0) return 0;
+  if (need_dev(in, "to_bf16 in") || need_dev(y, "to_bf16 y")) return -1;
   to_bf16_kernel<<<grid_for(V), 256, 0, (cudaStream_t)stream>>>(in, V, scale, (__nv_bfloat16 *)y,
                                                                 y_cstride, y_coff);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet to_bf16: launch failed");
@@ -1213,6 +1249,11 @@ int sepx_unet_to_bf16(const float *in, long long V, float scale, void *y, int y_
 
 int sepx_unet_mse(const float *out, const float *target, long long V, void *g, int g_cstride,
                   double *loss, void *stream) {
+  if (V < 0) return set_error("unet mse: negative length");
+  if (V == 0) return 0;
+  if (need_dev(out, "mse out") || need_dev(target, "mse target") || need_dev(g, "mse g") ||
+      need_dev(loss, "mse loss"))
+    return -1;
   mse_kernel<<<grid_for(V), 256, 0, (cudaStream_t)stream>>>(out, target, V, (__nv_bfloat16 *)g,
                                                             g_cstride, loss);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet mse: launch failed");
@@ -1220,6 +1261,10 @@ int sepx_unet_mse(const float *out, const float *target, long long V, void *g, i
 
 int sepx_unet_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1,
                    float b2, float eps, int step, void *stream) {
+  if (n < 0 || step < 1) return set_error("unet adam: n %lld, step %d", n, step);
+  if (n == 0) return 0;
+  if (need_dev(p, "adam p") || need_dev(g, "adam g") || need_dev(m, "adam m") || need_dev(v, "adam v"))
+    return -1;
   const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
   adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet adam: launch failed");

@@ -67,3 +67,27 @@ def test_device_vector_calls_reject_null_and_negative_lengths(raw):
     _rejects(L, L.sepx_dot_f32(fp, None, n(5), None), "NULL")
     _rejects(L, L.sepx_op_image_to_padded(None, 4, 4, 4, 0, 0, 0), "NULL")
     _rejects(L, L.sepx_op_traces_to_data(None, 10, C.c_float(0.001)), "NULL")
+
+
+def test_unet_calls_reject_null_operands(raw):
+    """A NULL device operand of the U-Net kernels is an error, not a launch
+    that reads address 0; an empty element-wise call is a no-op."""
+    L = raw
+    p = VP(16)   # never dereferenced: every call below fails or returns first
+    n = C.c_longlong
+    _rejects(L, L.sepx_unet_pack_weights(None, 8, 8, 27, 0, p, None), "NULL")
+    _rejects(L, L.sepx_unet_conv_fwd(None, 8, 0, 1, 4, 8, 8, 8, 27, p, None, 8, 0, p, 8, 0,
+                                     None, None, None), "NULL")
+    _rejects(L, L.sepx_unet_conv_fwd(p, 8, 0, 1, 4, 8, 8, 8, 27, None, None, 8, 0, p, 8, 0,
+                                     None, None, None), "NULL")
+    _rejects(L, L.sepx_unet_conv_fwd(p, 8, 0, 1, 4, 8, 8, 8, 27, p, None, 8, 0, None, 8, 0,
+                                     None, None, None), "no output")
+    _rejects(L, L.sepx_unet_conv_fwd(p, 8, 0, 0, 4, 8, 8, 8, 27, p, None, 8, 0, p, 8, 0,
+                                     None, None, None), "empty volume")
+    _rejects(L, L.sepx_unet_conv_wgrad(p, 8, 0, 1, 4, 8, 8, 8, 27, None, 8, 0, 8, p, None), "NULL")
+    _rejects(L, L.sepx_unet_avgpool(p, 8, 0, 1, 4, 8, 8, 8, None, 8, 0, None), "NULL")
+    _rejects(L, L.sepx_unet_upsample_bwd(None, 8, 0, 1, 4, 8, 8, 8, p, 8, 0, None), "NULL")
+    _rejects(L, L.sepx_unet_adam(p, None, p, p, n(8), C.c_float(1e-3), C.c_float(0.9),
+                                 C.c_float(0.999), C.c_float(1e-8), 1, None), "NULL")
+    _rejects(L, L.sepx_unet_mse(p, p, n(-1), p, 8, p, None), "negative length")
+    assert L.sepx_unet_to_bf16(None, n(0), C.c_float(1.0), None, 8, 0, None) == 0
