@@ -142,7 +142,7 @@ class ClockSampler:
 def build_workload(args):
     from sep_code_gb300 import model as M
     n1, n2, n3 = (int(v) for v in args.grid.split("x"))
-    s = M.config2_survey(n1, n2, n3, nt=args.nt)
+    s = M.layered_survey(n1, n2, n3, nt=args.nt)
     st = M.prepare_shot(s)
     return s, st
 
@@ -409,7 +409,7 @@ def run_batch(args):
     from sep_code_gb300 import batch as Bt
     nt = args.batch_nt
     t0 = time.perf_counter()
-    surveys = Bt.config4_surveys(nt=nt)
+    surveys = Bt.windowed_surveys(nt=nt)
     b = Bt.BatchRTM(surveys)
     t_setup = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(Bt.lib.sepx_get_stream())

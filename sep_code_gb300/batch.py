@@ -1,6 +1,6 @@
 """Many shots per time step (include/sepx_batch.h).
 
-``config4_surveys`` builds the batched workload: a 1024 x 1024 x 400 model
+``windowed_surveys`` builds the batched workload: a 1024 x 1024 x 400 model
 (the layered generator of the 512 x 512 x 400 workload), 16 shots on a
 jittered surface grid, each with its own aperture window from 192 x 192 x 256
 to 384 x 384 x 320 cells, receivers at every surface node of its window.
@@ -60,10 +60,10 @@ def window_surveys(vel, refl, d, centers, windows, nt, f0=20.0):
     return out
 
 
-def config4_surveys(nt: int = 1000, nshots: int = 16, model=(1024, 1024, 400), seed: int = 20261209):
+def windowed_surveys(nt: int = 1000, nshots: int = 16, model=(1024, 1024, 400), seed: int = 20261209):
     """16 shots, uneven windows 192^2 x 256 .. 384^2 x 320, jittered 4 x 4 grid"""
     n1, n2, n3 = model
-    big = M.config2_survey(n1, n2, n3, nt=8, seed=seed)
+    big = M.layered_survey(n1, n2, n3, nt=8, seed=seed)
     d = big.spacing[0]
     rng = np.random.default_rng(seed + 1)
     k = int(np.ceil(np.sqrt(nshots)))

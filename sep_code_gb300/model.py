@@ -43,7 +43,7 @@ def ricker(f0: float, dt: float, nt: int, t0: float | None = None) -> np.ndarray
     return ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
 
 
-def config1_survey(n: int = 128, nt: int = 1000, seed: int = 20261204) -> Survey:
+def anomaly_survey(n: int = 128, nt: int = 1000, seed: int = 20261204) -> Survey:
     """128^3, dx=10 m, dt=1 ms: v(z)=1500+0.6 z plus a +300 m/s Gaussian
     (sigma 150 m) at the centre; 5 flat horizons with N(0,0.05) amplitudes and
     ~2% sparse spikes; 15 Hz Ricker at the surface centre; receivers at every
@@ -63,10 +63,10 @@ def config1_survey(n: int = 128, nt: int = 1000, seed: int = 20261204) -> Survey
     w = ricker(15.0, 0.001, nt)
     return Survey(vel=vel.astype(np.float32), spacing=(d, d, d), refl=refl, wavelet=w, dtw=0.001,
                   data_nt=nt, data_dt=0.001, rec=(n, n, 0.0, d, 0.0, d),
-                  shots=[(c, c, 0.0)], nbound=20, name=f"config1_{n}")
+                  shots=[(c, c, 0.0)], nbound=20, name=f"anomaly_{n}")
 
 
-def config2_survey(n1: int = 512, n2: int = 512, n3: int = 400, nt: int = 4000,
+def layered_survey(n1: int = 512, n2: int = 512, n3: int = 400, nt: int = 4000,
                    seed: int = 20261205) -> Survey:
     """512x512x400, dx=12.5 m, dt=1 ms: seeded layered 1500-4500 m/s velocity
     with 8 random-depth dipping interfaces and smooth lateral perturbations;
@@ -97,7 +97,7 @@ def config2_survey(n1: int = 512, n2: int = 512, n3: int = 400, nt: int = 4000,
     return Survey(vel=vel, spacing=(d, d, d), refl=refl.astype(np.float32), wavelet=w, dtw=0.001,
                   data_nt=nt, data_dt=0.001, rec=(n1, n2, 0.0, d, 0.0, d),
                   shots=[((n1 - 1) * d / 2, (n2 - 1) * d / 2, 0.0)], nbound=20,
-                  name=f"config2_{n1}x{n2}x{n3}")
+                  name=f"layered_{n1}x{n2}x{n3}")
 
 
 def small_survey(m1=24, m2=20, m3=28, nt=60, d=10.0, nbound=4, seed=7, rnx=None, rny=None,

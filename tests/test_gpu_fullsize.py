@@ -25,7 +25,7 @@ def _chk(rc):
 
 def test_full_size_linearity():
     from sep_code_gb300 import model as M
-    s = M.config2_survey()
+    s = M.layered_survey()
     st = M.prepare_shot(s)
     n1, n2, n3 = st.n
     nrec = st.rnx * st.rny

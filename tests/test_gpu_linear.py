@@ -62,9 +62,9 @@ def test_lin_dot_product(prec):
 
 
 @pytest.mark.slow
-def test_lin_dot_product_config1():
+def test_lin_dot_product_128():
     """the 128^3, dx=10 m, dt=1 ms, 1000-step workload (padded 176x176x224)"""
-    s = M.config1_survey()
+    s = M.anomaly_survey()
     st = M.prepare_shot(s)
     c = LinCase(s, st)
     a, b = _dot_test(c, 1, "f32")
@@ -73,10 +73,10 @@ def test_lin_dot_product_config1():
 
 
 @pytest.mark.slow
-def test_lin_forward_repeatable_config1():
+def test_lin_forward_repeatable_128():
     """the same forward twice on the 128^3 workload (several CTAs per SM
     sharing tensor memory, 1000 steps): bit-identical traces"""
-    s = M.config1_survey()
+    s = M.anomaly_survey()
     st = M.prepare_shot(s)
     c = LinCase(s, st)
     m = np.random.default_rng(3).standard_normal((st.n[2], st.n[1], st.n[0])).astype(np.float32)

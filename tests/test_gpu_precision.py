@@ -76,7 +76,7 @@ def _oracle_image_f64(oracle, case, s, st, d):
 def test_snapshot_precision_vs_fp64(oracle):
     n = int(os.environ.get("SEPX_STUDY_N", "80"))
     nt = int(os.environ.get("SEPX_STUDY_NT", "500"))
-    s = M.config1_survey(n=n, nt=nt)
+    s = M.anomaly_survey(n=n, nt=nt)
     st = M.prepare_shot(s)
     case = LinCase(s, st)
     d = _data(case, s, st)
@@ -102,7 +102,7 @@ def test_snapshot_precision_vs_fp64(oracle):
 @pytest.mark.skipif(os.environ.get("SEPX_PRECISION_FULL") != "1",
                     reason="256^3 x 2500-step study: set SEPX_PRECISION_FULL=1")
 def test_snapshot_precision_full_size():
-    s = M.config1_survey(n=256, nt=2500, seed=20261206)
+    s = M.anomaly_survey(n=256, nt=2500, seed=20261206)
     st = M.prepare_shot(s)
     case = LinCase(s, st)
     d = _data(case, s, st)

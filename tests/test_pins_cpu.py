@@ -231,7 +231,7 @@ def test_oracle_born_forward_doubling(oracle):
     doubling the image doubles the traces to relative L2 ~1e-7..1e-6, not exactly
     (the bar the full-size GPU property test uses is 1e-5)."""
     from tests.harness import OracleShot, rel_l2
-    s = M.config1_survey(n=32, nt=250)
+    s = M.anomaly_survey(n=32, nt=250)
     st = M.prepare_shot(s)
     o = OracleShot(oracle, s, st)
     d1 = o.rtm_forward(st.img_lap)
