@@ -41,7 +41,8 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nt", type=int, default=4000, help="propagation steps (the workload's 4000)")
     p.add_argument("--grid", default="512x512x400")
-    p.add_argument("--cpu-sample-steps", type=int, default=10)
+    # 25 steps of each loop on the full grid: about 13 s of CPU work on 16 cores
+    p.add_argument("--cpu-sample-steps", type=int, default=25)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", default="rtm", choices=["rtm", "batch"],
