@@ -141,11 +141,35 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ workload
 def build_workload(args):
+    """The survey and the product's own shot set-up (GPU arm)."""
     from sep_code_gb300 import model as M
+    from sep_code_gb300 import surveys as S
     n1, n2, n3 = (int(v) for v in args.grid.split("x"))
-    s = M.layered_survey(n1, n2, n3, nt=args.nt)
-    st = M.prepare_shot(s)
-    return s, st
+    s = S.layered_survey(n1, n2, n3, nt=args.nt)
+    return s, M.prepare_shot(s)
+
+
+def build_workload_oracle(args, orc):
+    """The same survey and shot set-up from the oracle alone (CPU arm): no
+    product library is loaded on this path."""
+    from oracle.shot_setup import prepare_shot
+    from sep_code_gb300 import surveys as S
+    n1, n2, n3 = (int(v) for v in args.grid.split("x"))
+    s = S.layered_survey(n1, n2, n3, nt=args.nt)
+    return s, prepare_shot(orc, s)
+
+
+def workload_config(args, st, ws):
+    """The ``config`` object of both arms' JSON lines (identical keys)."""
+    n1, n2, n3 = st.n
+    cells, fsteps = cell_updates(st)
+    return {"workload": f"rtm_single_shot_{args.grid}_nt{st.nt}",
+            "model_grid": args.grid, "padded_grid": f"{n1}x{n2}x{n3}", "dx_m": st.d[0],
+            "dt_s": st.dt, "nt": st.nt, "receivers": st.rnx * st.rny,
+            "cells_per_field_step": cells, "field_steps_per_step": fsteps,
+            "l2": "inputs larger than L2 (each volume "
+                  f"{4 * n1 * n2 * n3 / 1e6:.0f} MB > 129 MB)",
+            "parallelism": f"{ws} independent shot(s), one per GPU"}
 
 
 def cell_updates(st):
@@ -175,22 +199,17 @@ def profiled_traffic(kernel_key: str):
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle)
-def cpu_baseline(s, st, steps, threads=None):
+def cpu_baseline(s, st, steps, orc=None):
     """The reference path's CPU restatement (oracle/) on a bounded sample: the
-    three time loops of the workload, ``steps`` time steps each, full grid."""
-    from oracle.bindings import Oracle, damp_ntab
-    from sep_code_gb300 import gpu_funcs as gf
-    orc = Oracle()
-    if threads:
-        orc.set_num_threads(threads)
+    three time loops of the workload, ``steps`` time steps each, full grid,
+    all host threads.  Inputs come from the oracle's own set-up routines."""
+    from oracle.bindings import Oracle
+    from oracle.shot_setup import make_ctx, source_vals
+    orc = orc or Oracle()
     n1, n2, n3 = st.n
     keep = []
-    wd = gf.wavelet_deriv(s.wavelet, s.dtw)
-    sx, sy, sz = s.shots[0]
-    locs, vals = gf.source_func(wd, sx, sy, sz, n1, n2, st.o, st.d, s.data_nt + 9)
-    ctx = orc.make_ctx(st.n, orc.fd_coeffs(*st.d), orc.damp_table(s.bc_a, s.bc_b, damp_ntab(n1, n2, n3)),
-                       vals.shape[1], st.sinc_s, st.sinc_d, locs, vals,
-                       np.ascontiguousarray(st.rec_locs, np.int32), st.rnx, st.rny, keep)
+    locs, vals = source_vals(orc, s, st, 9)
+    ctx = make_ctx(orc, s, st, locs, vals, keep)
     nrec = st.rnx * st.rny
     dat = np.zeros((nrec, vals.shape[1]), np.float32)
     img = np.ascontiguousarray(st.img_lap, np.float32)
@@ -385,13 +404,7 @@ def run_ours(args, ws, rank, dist):
         "warmup": args.warmup, "ms_per_step": round(elapsed_max / args.steps * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded layered 1500-4500 m/s model, 8 dipping interfaces, 20 Hz Ricker)",
-        "config": {"workload": f"rtm_single_shot_{args.grid}_nt{st.nt}",
-                   "model_grid": args.grid, "padded_grid": f"{n1}x{n2}x{n3}", "dx_m": st.d[0],
-                   "dt_s": st.dt, "nt": st.nt, "receivers": nrec,
-                   "cells_per_field_step": cells, "field_steps_per_step": fsteps,
-                   "l2": "inputs larger than L2 (each volume "
-                         f"{4 * n1 * n2 * n3 / 1e6:.0f} MB > 129 MB)",
-                   "parallelism": f"{ws} independent shot(s), one per GPU"},
+        "config": workload_config(args, st, ws),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -456,17 +469,20 @@ def run_batch(args):
 # ------------------------------------------------------------------ reference arm
 def run_reference(args, ws, rank):
     """The reference has no CPU propagation; its CPU path is the oracle's
-    restatement (oracle/), timed on the host cores with all threads."""
+    restatement (oracle/), timed on the host cores with all threads.  Survey,
+    random boundary, sinc tables and source stencil come from the oracle's
+    own set-up routines: this arm loads no product library."""
     if rank != 0:
         return
-    s, st = build_workload(args)
-    cells, fsteps = cell_updates(st)
+    from oracle.bindings import Oracle
+    orc = Oracle()
+    s, st = build_workload_oracle(args, orc)
     for _ in range(args.warmup):
-        cpu_baseline(s, st, max(1, args.cpu_sample_steps // 2))
+        cpu_baseline(s, st, max(1, args.cpu_sample_steps // 2), orc)
     vals = []
     secs = 0.0
     for _ in range(args.steps):
-        r = cpu_baseline(s, st, args.cpu_sample_steps)
+        r = cpu_baseline(s, st, args.cpu_sample_steps, orc)
         vals.append(r["value"])
         secs += r["seconds"]
     v = float(np.mean(vals))
@@ -477,12 +493,10 @@ def run_reference(args, ws, rank):
         "value": round(v, 4), "unit": "Gcell/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded layered model)",
-        "config": {"workload": f"rtm_single_shot_{args.grid}_nt{st.nt}",
-                   "padded_grid": "x".join(map(str, st.n)),
-                   "sample": f"{args.cpu_sample_steps} time steps of each loop per step"},
+        "data": "synthetic (seeded layered 1500-4500 m/s model, 8 dipping interfaces, 20 Hz Ricker)",
+        "config": workload_config(args, st, ws),
         "cpu_baseline": {"value": round(v, 4), "unit": "Gcell/s", "cores": r["cores"],
-                         "kind": "port", "sample": r["sample"]},
+                         "kind": "port", "sample": r["sample"] + " per step"},
         "e2e": {"value": round(v, 4), "unit": "Gcell/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }

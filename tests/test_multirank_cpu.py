@@ -61,3 +61,25 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm builds its survey, random boundary, sinc tables and
+    source stencil from the oracle: libsepx.so is never mapped and no module
+    of the product that binds it is imported."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '0', '--grid', '24x24x24', '--nt', '20', '--cpu-sample-steps', '2']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPPED', 'libsepx.so' in maps, 'libsepx_oracle.so' in maps); "
+            "print('MODS', sorted(m for m in sys.modules if m.startswith('sep_code_gb300')))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = r.stdout.splitlines()
+    assert "MAPPED False True" in out, r.stdout
+    mods = [ln for ln in out if ln.startswith("MODS")][0]
+    assert "_lib" not in mods and "gpu_funcs" not in mods and "model" not in mods.replace(
+        "sep_code_gb300.surveys", ""), mods
+    line = json.loads([ln for ln in out if ln.startswith("{")][0])
+    assert line["impl"] == "reference" and line["config"]["padded_grid"]
