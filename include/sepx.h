@@ -187,6 +187,10 @@ const char *sepx_last_error(void);
 int sepx_device_error(void);          /* device error word (bounded waits), then cleared */
 long long sepx_kernel_launches(void); /* kernels launched by this library so far */
 int sepx_set_zchunk(int planes);      /* z planes per CTA; 0 = automatic */
+/* Rows per consumer thread of a step kernel (tuning knob): mode 0 =
+   source_prop, 1 = Born forward, 2 = RTM adjoint steps; rows 1 (tile 32 x 16,
+   the default) or 2 (tile 32 x 32).  Both give identical results. */
+int sepx_set_tile_rows(int mode, int rows);
 int sepx_reset(void);                 /* free every device buffer */
 
 #ifdef __cplusplus

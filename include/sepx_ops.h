@@ -21,7 +21,7 @@ extern "C" {
 typedef struct {
   const float *vel;          /* model velocity, host float[m3][m2][m1] (m/s) */
   int m1, m2, m3;
-  float d1, d2, d3;          /* grid spacing; origins 0 */
+  float d1, d2, d3;          /* grid spacing (origins: mo1..mo3 below) */
   const float *wavelet;      /* source wavelet before its time derivative */
   int nwav;
   float dtw;
@@ -38,6 +38,7 @@ typedef struct {
                                 1: the exact-adjoint linearised pair */
   int snap_js;               /* mode 1: snapshot interval (steps) */
   int snap_prec;             /* mode 1: 0 FP32, 1 BF16, 2 FP16 */
+  float mo1, mo2, mo3;       /* origins of the velocity / image grid (0 if unset) */
 } sepx_rtm_problem;
 
 typedef void *sepx_op_handle;
@@ -96,6 +97,7 @@ int sepx_lsrtm_ex(sepx_op_handle op, const float *data, int niter, const sepx_ls
 #ifdef __cplusplus
 }
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -289,11 +291,72 @@ class reg_solver : public lin_solver {
              my_vector *m0 = nullptr);
 };
 
+// ---- the reference's input objects of rtm_zero_op, without SEPlib ----
+
+// Named parameters (Born/param_func.h): the operator reads bc_a (default 50),
+// bc_b (0.0005), nbound (int(bc_a)) and rec_depth (0).  The reference's
+// values come from the command line through SEPlib; here they are set in
+// code.
+class param_func {
+ public:
+  virtual ~param_func() {}
+  virtual int get_int(const char *arg, int def) const;
+  virtual float get_float(const char *arg, float def) const;
+  param_func &set(const std::string &name, double value);
+  std::map<std::string, double> vals;
+};
+
+// Velocity model on its grid (Born/vel_fd_3d.h), in host memory: every shot
+// resamples it onto its padded grid with the random boundary.
+class vel_fd_3d {
+ public:
+  vel_fd_3d(const std::vector<axis> &axes, const float *vel);
+  axis get_axis(int iax) const { return axes[iax - 1]; }
+  float max_vel() const;
+  float min_vel() const;
+  // the reference's rules, including dz returned when dy < dx
+  // (Born/vel_fd_3d.h:11-26)
+  float get_min_samp() const;
+  float get_max_samp() const;
+  std::vector<axis> axes;
+  std::vector<float> vals;
+};
+
+// Source wavelet and shot positions (Born/source_func_3d.h).  The wavelet is
+// given as recorded; its time derivative (Born/source_func_3d.cpp:4-20) is
+// taken by the operator.
+class source_func {
+ public:
+  source_func(axis at, const float *wavelet);
+  // one shot per (sx, sy) node of the two axes at depth s_z, x fastest
+  // (Born/source_func_3d.cpp:22-33)
+  void set_sources_3d(float s_z, axis a_sx, axis a_sy);
+  int get_points(bool) const { return 9; }
+  float get_dt() const { return at.d; }
+  axis get_axis(int) const { return at; }
+  axis at;
+  std::vector<float> wavelet, sx, sy, sz;
+};
+
+class data_rtm_3d;
+class image_rtm_3d;
+
 // The Born / RTM operator (Born/rtm_zero_op_3d.h).  Model: image on the model
 // grid float[m3][m2][m1]; data: float[nshots][rny][rnx][data_nt].
 class rtm_zero_op : public my_operator {
  public:
   explicit rtm_zero_op(const sepx_rtm_problem &p);
+  // The reference's constructor (Born/rtm_zero_op_3d.cpp:8-36): the data
+  // axes (t, receiver x, receiver y, shots ...) give the recording and the
+  // receiver grid, the source the wavelet and the shot positions (one per
+  // trace gather of `data`), the image the model grid (the operator's
+  // domain is image->image, its range `data`).  do_src: propagate the
+  // source wavefields now (else at the first adjoint); redo_src: propagate
+  // them again at every adjoint.  aper, encode and rand_vec are accepted for
+  // the signature: the reference's forward and adjoint do not use them.
+  rtm_zero_op(param_func *par, vel_fd_3d *vel, source_func *source, data_rtm_3d *data,
+              image_rtm_3d *image, float aper, bool verb, bool encode, int *rand_vec,
+              bool do_src = true, bool redo_src = false);
   ~rtm_zero_op() override;
   bool forward(bool add, my_vector *model, my_vector *data, int iter = 1) override;
   bool adjoint(bool add, my_vector *model, my_vector *data, int iter = 1) override;
@@ -303,6 +366,9 @@ class rtm_zero_op : public my_operator {
   struct shot_setup;
   struct impl;
   impl *d = nullptr;
+
+ private:
+  void init(const sepx_rtm_problem &p);
 };
 
 // Time mute (Born/tmute.h, Born/tmute.cpp:4-76): the samples of trace i2 from
@@ -324,7 +390,11 @@ class tmute : public my_operator {
 class image_rtm_3d {
  public:
   explicit image_rtm_3d(const std::vector<axis> &axes);
+  // the image on the velocity model's grid, zero (Born/image_rtm_3d.cpp:4-16)
+  image_rtm_3d(const char *tag, const vel_fd_3d *vel);
   ~image_rtm_3d();
+  void zero() { image->zero(); }
+  void add(my_vector *v) { image->add(v); }
   image_rtm_3d(const image_rtm_3d &) = delete;
   void set_mute(const hypercube_float &m);          // copies m (same shape)
   void add_image(const hypercube_float *img);       // image_rtm_3d.cpp:24-49
@@ -339,7 +409,10 @@ class image_rtm_3d {
 class data_rtm_3d : public hypercube_float {
  public:
   explicit data_rtm_3d(const std::vector<axis> &axes);
+  // with the receiver depth parameter rec_depth (Born/data_rtm_3d.cpp:4-20)
+  data_rtm_3d(const std::vector<axis> &axes, const param_func *par);
   void add_data(int ishot, const hypercube_float *dat);
+  float sz = 0.f;   // receiver depth
   int nshots() const;   // product of the axes after the third
 };
 

@@ -103,6 +103,10 @@ class Oracle:
                                           F64P, F64P, F64P]
         L.orc_lin_forward_f64.argtypes = [C.POINTER(OrcCtx64), F64P, C.c_int, C.c_int, C.c_int,
                                           C.c_int, F64P, F64P]
+        L.orc_lin_adjoint_ckpt_f32.argtypes = [C.POINTER(OrcCtx), F32P, C.c_int, C.c_int, C.c_int,
+                                               C.c_int, C.c_int, C.c_int, F32P, F32P]
+        L.orc_lin_adjoint_ckpt_f64.argtypes = [C.POINTER(OrcCtx64), F64P, C.c_int, C.c_int, C.c_int,
+                                               C.c_int, C.c_int, F64P, F64P]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
 

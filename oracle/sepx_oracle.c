@@ -542,6 +542,16 @@ int orc_lin_adjoint_f32(const orc_ctx *c, const float *vel, int jt, int nt, int 
                         const float *snaps, const float *dat, float *img) {
   return lin_adjoint_impl_f32(c, vel, jt, nt, js, snaps, dat, img);
 }
+int orc_lin_adjoint_ckpt_f32(const orc_ctx *c, const float *vel, int jt, int npts, int nt, int js,
+                             int prec, int seg, const float *dat, float *img) {
+  return lin_adjoint_ckpt_impl_f32(c, vel, jt, npts, nt, js, prec, seg, dat, img);
+}
+int orc_lin_adjoint_ckpt_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt,
+                             int js, int seg, const double *dat, double *img) {
+  ctx64_full f;
+  fill64(c, &f);
+  return lin_adjoint_ckpt_impl_f64(&f, vel, jt, npts, nt, js, 0, seg, dat, img);
+}
 int orc_lin_source_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt, int js,
                        double *snaps) {
   ctx64_full f;

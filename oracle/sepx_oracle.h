@@ -136,6 +136,14 @@ int orc_lin_forward_f64(const orc_ctx64 *c, const double *vel, int jt, int npts,
                         const double *m, double *dat);
 int orc_lin_adjoint_f64(const orc_ctx64 *c, const double *vel, int jt, int nt, int js,
                         const double *snaps, const double *dat, double *img);
+/* source pass and adjoint in one call, the source wavefield recomputed from
+ * checkpoints every seg steps instead of stored (same image as
+ * orc_lin_source_* + orc_lin_adjoint_*; 2 ceil(nt/seg) + ceil(seg/js) + 7
+ * volumes of memory) */
+int orc_lin_adjoint_ckpt_f32(const orc_ctx *c, const float *vel, int jt, int npts, int nt, int js,
+                             int prec, int seg, const float *dat, float *img);
+int orc_lin_adjoint_ckpt_f64(const orc_ctx64 *c, const double *vel, int jt, int npts, int nt,
+                             int js, int seg, const double *dat, double *img);
 
 /* threads used by the OpenMP loops */
 int orc_num_threads(void);

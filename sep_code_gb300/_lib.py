@@ -52,6 +52,7 @@ def _load() -> C.CDLL:
         "sepx_zero_traces": [],
         "sepx_device_error": [],
         "sepx_set_zchunk": [i],
+        "sepx_set_tile_rows": [i, i],
         "sepx_reset": [],
         "sepx_lin_source_pass": [i, i, i, i, i],
         "sepx_lin_forward_resident": [i, i, i, i, i],

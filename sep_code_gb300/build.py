@@ -41,6 +41,7 @@ def _sources() -> list[Path]:
 
 def _deps() -> list[Path]:
     return _sources() + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + \
+        sorted(CSRC.glob("*.inc")) + \
         sorted(INCLUDE.glob("*.h")) + [Path(__file__)]
 
 

@@ -8,6 +8,9 @@ namespace sepx {
 
 cudaError_t launch_prop_step(int mode, const PropParams &P, cudaStream_t st);
 size_t prop_smem_bytes(int mode);
+// two-row tile (kSrcProp, kBornFwd, kRtmAdj): 32 x 32 cells per CTA
+cudaError_t launch_prop_step2(int mode, const PropParams &P, const Rows2Maps &H, cudaStream_t st);
+bool prop_step2_supported(int mode);
 // persistent multi-grid launches (sepx_prop.cu): stages 3 or 4
 bool batch_supported(int mode, int stages);
 cudaError_t launch_prop_batch(int mode, int stages, const PropParams *params, const int4 *items,

@@ -39,6 +39,7 @@ struct Volume {
   float *base = nullptr;
   float *origin = nullptr;
   CUtensorMap tm_h, tm_c;
+  CUtensorMap tm_h2;   // 40 x 40 halo box of the two-row tile
 };
 
 struct PointMapDev {
@@ -56,6 +57,10 @@ struct Ctx {
   int *d_err = nullptr;
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   int zchunk_override = 0;
+  // modes (bit per PropMode) that run the two-row tile (32 x 32 cells per
+  // CTA): none by default -- on GB300 at 560 x 560 x 496 it measured slower
+  // than the one-row tile for every mode (2 CTAs per SM instead of 4)
+  int rows2_mask = 0;
   int num_sms = 152;
   // grid
   bool have_grid = false;
@@ -211,6 +216,7 @@ int alloc_volume(Volume &v) {
   v.origin = v.base + kLead;
   RET(encode_map(&v.tm_h, v.origin, kHX, kHY));
   RET(encode_map(&v.tm_c, v.origin, kTX, kTY));
+  RET(encode_map(&v.tm_h2, v.origin, kHX, kHY2));
   return 0;
 }
 
@@ -317,9 +323,27 @@ int auto_zchunk(int mode) {
   return std::max(1, std::min(zc, depth));
 }
 
-// One fused step with the mode's z-chunk.
-cudaError_t launch_step(int mode, const PropParams &P0) {
+// The same for the two-row tile (32 x 32 cells, 2 CTAs per SM): the chunk
+// count of the target length, planes spread evenly over the chunks.
+int auto_zchunk2(int mode) {
+  if (G.zchunk_override > 0) return G.zchunk_override;
+  const PropGeom &g = G.geom;
+  const long long tiles = (long long)((g.xe - g.xb + kTX - 1) / kTX) * ((g.ye - g.yb + kTY2 - 1) / kTY2);
+  const int depth = std::max(1, g.ze - g.zb);
+  int zc = (mode == kRtmAdj) ? 32 : 80;
+  while (zc > 16 && tiles * ((depth + zc - 1) / zc) < 2LL * 2 * G.num_sms) zc /= 2;
+  const int nch = (depth + zc - 1) / zc;
+  return std::max(1, std::min((depth + nch - 1) / nch, depth));
+}
+
+// One fused step with the mode's z-chunk; modes in rows2_mask take the
+// two-row tile when the 40 x 40 halo maps are given.
+cudaError_t launch_step(int mode, const PropParams &P0, const Rows2Maps *H = nullptr) {
   PropParams P = P0;
+  if (H && ((G.rows2_mask >> mode) & 1) && prop_step2_supported(mode)) {
+    P.g.zchunk = auto_zchunk2(mode);
+    return launch_prop_step2(mode, P, *H, G.stream);
+  }
   P.g.zchunk = auto_zchunk(mode);
   return launch_prop_step(mode, P, G.stream);
 }
@@ -395,14 +419,17 @@ int loop_source_prop(int jt, int npts, int nt) {
   RET(zero_volume(*A));
   RET(zero_volume(*B));
   PropParams P = base_params();
+  Rows2Maps H;
+  H.vel_h = G.vel.tm_h2;
   P.src.plane_slot = G.srcmap.plane_slot;
   P.src.map = G.srcmap.map;
   P.src.next = G.srcmap.next;
   for (int it = 0; it <= nt; it++) {
     set_field(P, 0, *B, *A);
+    H.cur_h[0] = B->tm_h2;
     P.inj_s = G.d_inj + (size_t)it * std::max(npts, 0);
     if (npts <= 0) P.src.plane_slot = nullptr;
-    CKL(launch_step(kSrcProp, P));
+    CKL(launch_step(kSrcProp, P, &H));
     std::swap(A, B);
   }
   G.sl_p0 = (A == &G.SL[0]) ? 0 : 1;
@@ -428,15 +455,19 @@ int loop_rtm_forward(int jt, int npts_src, int nt) {
   P.rec.next = G.recmap.next;
   P.trc = G.d_trc;
   P.nrec = G.rec_nx * G.rec_ny;
+  Rows2Maps H;
+  H.vel_h = G.vel.tm_h2;
   for (int it = 0; it < nt; it++) {
     const int id = it / jt, ii = it - id * jt;
     set_field(P, 0, *D1, *D0);
     set_field(P, 1, *S1, *S0);
+    H.cur_h[0] = D1->tm_h2;
+    H.cur_h[1] = S1->tm_h2;
     P.inj_s = G.d_inj + (size_t)it * std::max(npts_src, 0);
     P.do_scatter = (it % jt == 0);
     P.trc_id = id;
     P.sinc_row = G.d_sinc_d + (size_t)ii * G.nsinc;
-    CKL(launch_step(kBornFwd, P));
+    CKL(launch_step(kBornFwd, P, &H));
     std::swap(D0, D1);
     std::swap(S0, S1);
   }
@@ -460,6 +491,8 @@ int loop_rtm_adjoint(int jt, int npts, int nt) {
   P.rec.next = G.recmap.next;
   P.trc = G.d_trc;
   P.nrec = G.rec_nx * G.rec_ny;
+  Rows2Maps H;
+  H.vel_h = G.vel.tm_h2;
   for (int it = nt - 1; it >= 0; it--) {
     const int id = it / jt, ii = it - id * jt;
     P.trc_id = id;
@@ -471,7 +504,9 @@ int loop_rtm_adjoint(int jt, int npts, int nt) {
       CKL(launch_step(kRtmAdj1, P));
     } else {
       set_field(P, 1, *S1, *S0);
-      CKL(launch_step(kRtmAdj, P));
+      H.cur_h[0] = D1->tm_h2;
+      H.cur_h[1] = S1->tm_h2;
+      CKL(launch_step(kRtmAdj, P, &H));
       if (npts > 0)
         CKL(launch_point_add(S1->origin, G.srcmap.off, G.d_inj + (size_t)it * npts, npts, G.stream));
       std::swap(S0, S1);
@@ -1166,6 +1201,18 @@ long long sepx_kernel_launches(void) { return g_launches; }
 int sepx_set_zchunk(int planes) {
   if (planes < 0) return fail("zchunk must be >= 0");
   G.zchunk_override = planes;
+  return 0;
+}
+
+int sepx_set_tile_rows(int mode, int rows) {
+  if (mode < 0 || mode > kLinAdj) return fail("unknown propagation mode %d", mode);
+  if (rows != 1 && rows != 2) return fail("rows per thread must be 1 or 2 (got %d)", rows);
+  if (rows == 2 && !prop_step2_supported(mode))
+    return fail("mode %d has no two-row tile (only source_prop, Born forward and RTM adjoint steps)", mode);
+  if (rows == 2)
+    G.rows2_mask |= 1 << mode;
+  else
+    G.rows2_mask &= ~(1 << mode);
   return 0;
 }
 

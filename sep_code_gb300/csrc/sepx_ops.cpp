@@ -4,6 +4,7 @@
 // set-up follows rtm_zero_op (Born/rtm_zero_op_3d.cpp) with in-memory inputs.
 #include "../../include/sepx_ops.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -51,6 +52,10 @@ hypercube_float::hypercube_float(const std::vector<axis> &ax) : axes(ax) {
   name = "hypercube_float";
   n123 = 1;
   for (const auto &a : axes) n123 *= a.n;
+  // the first device vector brings up the GPU (setup_cuda(1) does nothing
+  // once it has run), so vectors may be built before the program's own
+  // setup_cuda call, as the reference's programs build theirs
+  ck(sepx_setup_cuda(1), "setup_cuda");
   ck(sepx_vec_alloc(&vals, n123), "hypercube_float alloc");
   ck(sepx_vec_fill(vals, n123, 0.f), "hypercube_float fill");
 }
@@ -447,6 +452,8 @@ struct rtm_zero_op::impl {
   std::vector<float> sinc_s, sinc_d;
   std::vector<shot_setup> shots;
   bool fields_ready = false;
+  bool verb = false;   // progress lines on stderr
+  bool redo = false;   // propagate the source wavefields again at every adjoint
 
   void upload_tables() {
     std::vector<float *> rs(jts), rd(jtd);
@@ -470,8 +477,8 @@ struct rtm_zero_op::impl {
                           o[1], o[2], d[0], d[1], d[2], nt_big + 1, l9.data(), s.vals9.data());
     const int seed = s.src_locs[3] - (s.src_locs[3] / 10000) * 10000;
     s.vrand.resize((size_t)n1 * n2 * n3);
-    sepx_host_rand_subspace(seed, p.nbound, p.nbound, p.nbound, dt, vel.data(), p.m1, p.m2, p.m3, 0.f,
-                            0.f, 0.f, p.d1, p.d2, p.d3, n1, n2, n3, o[0], o[1], o[2], d[0], d[1],
+    sepx_host_rand_subspace(seed, p.nbound, p.nbound, p.nbound, dt, vel.data(), p.m1, p.m2, p.m3, p.mo1,
+                            p.mo2, p.mo3, p.d1, p.d2, p.d3, n1, n2, n3, o[0], o[1], o[2], d[0], d[1],
                             d[2], s.vrand.data());
     s.rec_locs.resize(nrec);
     sepx_host_receiver_map(p.rnx, p.rny, p.ro2, p.rd2, p.ro3, p.rd3, p.rec_depth, n1, n2, o[0],
@@ -482,6 +489,64 @@ struct rtm_zero_op::impl {
 };
 
 rtm_zero_op::rtm_zero_op(const sepx_rtm_problem &p) : d(new impl) {
+  init(p);
+  if (p.mode == 0) create_source_fields();
+}
+
+// Born/rtm_zero_op_3d.cpp:8-36 with fd_prop::set_fd_basics
+// (Born/fd_prop_3d.cpp:35-55): parameters bc_a, bc_b, nbound; receiver depth
+// rec_depth; the padded grid, stability, sinc tables and device grid.
+rtm_zero_op::rtm_zero_op(param_func *par, vel_fd_3d *vel, source_func *source, data_rtm_3d *data,
+                         image_rtm_3d *image, float /*aper*/, bool verb, bool /*encode*/,
+                         int * /*rand_vec*/, bool do_src, bool redo_src)
+    : d(new impl) {
+  if (!par || !vel || !source || !data || !image)
+    throw std::runtime_error("rtm_zero_op: NULL argument");
+  if (vel->axes.size() != 3) throw std::runtime_error("rtm_zero_op: the velocity needs three axes");
+  if (data->axes.size() < 3)
+    throw std::runtime_error("rtm_zero_op: the data needs (t, x, y[, shots]) axes");
+  const int nshots = data->nshots();
+  if ((int)source->sx.size() != nshots)
+    throw std::runtime_error("rtm_zero_op: " + std::to_string(source->sx.size()) +
+                             " source positions for " + std::to_string(nshots) + " shots of data");
+  for (int k = 1; k <= 3; k++) {
+    const axis a = image->get_axis(k), v = vel->get_axis(k);
+    if (a.n != v.n || a.o != v.o || a.d != v.d)
+      throw std::runtime_error("rtm_zero_op: the image grid differs from the velocity grid");
+  }
+  std::vector<float> xyz(3 * (size_t)nshots);
+  for (int i = 0; i < nshots; i++) {
+    xyz[3 * i] = source->sx[i];
+    xyz[3 * i + 1] = source->sy[i];
+    xyz[3 * i + 2] = source->sz[i];
+  }
+  sepx_rtm_problem p;
+  std::memset(&p, 0, sizeof p);
+  p.vel = vel->vals.data();
+  p.m1 = vel->axes[0].n; p.m2 = vel->axes[1].n; p.m3 = vel->axes[2].n;
+  p.d1 = vel->axes[0].d; p.d2 = vel->axes[1].d; p.d3 = vel->axes[2].d;
+  p.mo1 = vel->axes[0].o; p.mo2 = vel->axes[1].o; p.mo3 = vel->axes[2].o;
+  p.wavelet = source->wavelet.data();
+  p.nwav = (int)source->wavelet.size();
+  p.dtw = source->get_dt();
+  p.data_nt = data->axes[0].n;
+  p.data_dt = data->axes[0].d;
+  p.rnx = data->axes[1].n; p.ro2 = data->axes[1].o; p.rd2 = data->axes[1].d;
+  p.rny = data->axes[2].n; p.ro3 = data->axes[2].o; p.rd3 = data->axes[2].d;
+  p.rec_depth = par->get_float("rec_depth", data->sz);
+  p.nshots = nshots;
+  p.shot_xyz = xyz.data();
+  p.bc_a = par->get_float("bc_a", 50.f);
+  p.bc_b = par->get_float("bc_b", .0005f);
+  p.nbound = par->get_int("nbound", (int)p.bc_a);
+  p.mode = 0;
+  init(p);
+  d->verb = verb;
+  d->redo = redo_src;
+  if (do_src && !redo_src) create_source_fields();
+}
+
+void rtm_zero_op::init(const sepx_rtm_problem &p) {
   impl &I = *d;
   I.p = p;
   const long long nm = (long long)p.m1 * p.m2 * p.m3;
@@ -490,6 +555,10 @@ rtm_zero_op::rtm_zero_op(const sepx_rtm_problem &p) : d(new impl) {
   I.wavelet_deriv.resize(p.nwav);
   sepx_host_wavelet_deriv(w.data(), p.nwav, p.dtw, I.wavelet_deriv.data());
   I.shot_xyz.assign(p.shot_xyz, p.shot_xyz + 3 * p.nshots);
+  // the caller's arrays are copied: keep no pointer to them
+  I.p.vel = I.vel.data();
+  I.p.wavelet = nullptr;
+  I.p.shot_xyz = I.shot_xyz.data();
   // fd_prop::calc_stability (Born/fd_prop_3d.cpp:7-26) with vel_fd_3d's
   // get_min_samp (it returns dz when dy < dx, Born/vel_fd_3d.h:17)
   double vmax = I.vel[0];
@@ -507,9 +576,12 @@ rtm_zero_op::rtm_zero_op(const sepx_rtm_problem &p) : d(new impl) {
   sepx_host_compute_size(p.m1, p.m2, p.m3, p.nbound, p.nbound, p.nbound, 4, &I.n1, &I.n2, &I.n3);
   const int nb = p.nbound + 4;
   I.d[0] = p.d1; I.d[1] = p.d2; I.d[2] = p.d3;
+  const float mo[3] = {p.mo1, p.mo2, p.mo3};
   for (int k = 0; k < 3; k++) {
     I.o[k] = -I.d[k] * (float)nb;
-    I.f[k] = (int)(I.o[k] / I.d[k]);   // image_rtm_3d: model index = padded index + f
+    // image_rtm_3d::extract_sub (Born/image_rtm_3d.cpp:52-90): model index =
+    // padded index + f, f = (int)((o_padded - o_model) / d_model)
+    I.f[k] = (int)((I.o[k] - mo[k]) / I.d[k]);
   }
   I.sinc_s.resize((size_t)I.jts * 8);
   I.sinc_d.resize((size_t)I.jtd * 8);
@@ -523,14 +595,13 @@ rtm_zero_op::rtm_zero_op(const sepx_rtm_problem &p) : d(new impl) {
   std::unique_ptr<hypercube_float> m0(new_model()), d0(new_data());
   set_domain(m0.get());
   set_range(d0.get());
-  if (p.mode == 0) create_source_fields();
 }
 
 rtm_zero_op::~rtm_zero_op() { delete d; }
 
 hypercube_float *rtm_zero_op::new_model() const {
-  return new hypercube_float({axis(d->p.m1, 0.f, d->p.d1), axis(d->p.m2, 0.f, d->p.d2),
-                              axis(d->p.m3, 0.f, d->p.d3)});
+  return new hypercube_float({axis(d->p.m1, d->p.mo1, d->p.d1), axis(d->p.m2, d->p.mo2, d->p.d2),
+                              axis(d->p.m3, d->p.mo3, d->p.d3)});
 }
 
 hypercube_float *rtm_zero_op::new_data() const {
@@ -563,6 +634,7 @@ bool rtm_zero_op::forward(bool add, my_vector *model, my_vector *data, int) {
   if (!add) dv->zero();
   const long long slab = (long long)I.nrec * I.p.data_nt;
   for (int is = 0; is < I.p.nshots; is++) {
+    if (I.verb) fprintf(stderr, "Forward shot %d of %d\n", is, I.p.nshots);
     shot_setup &s = I.shot(is);
     ck(sepx_transfer_source_func(9, I.nt_big, s.src_locs.data(), s.vals8.data()), "transfer_source_func");
     ck(sepx_transfer_vel_func1(I.n1, I.n2, I.n3, s.vrand.data()), "transfer_vel_func1");
@@ -582,10 +654,12 @@ bool rtm_zero_op::forward(bool add, my_vector *model, my_vector *data, int) {
 // Born/rtm_zero_op_3d.cpp:185-293
 bool rtm_zero_op::adjoint(bool add, my_vector *model, my_vector *data, int) {
   impl &I = *d;
+  if (I.redo && I.p.mode == 0) create_source_fields();
   auto *m = hf(model), *dv = hf(data);
   if (!add) m->zero();
   const long long slab = (long long)I.nrec * I.p.data_nt;
   for (int is = 0; is < I.p.nshots; is++) {
+    if (I.verb) fprintf(stderr, "Adjoint shot %d of %d\n", is, I.p.nshots);
     shot_setup &s = I.shot(is);
     ck(sepx_transfer_source_func(9, I.nt_big, s.src_locs.data(), s.vals8.data()), "transfer_source_func");
     ck(sepx_transfer_vel_func1(I.n1, I.n2, I.n3, s.vrand.data()), "transfer_vel_func1");
@@ -794,6 +868,74 @@ image_rtm_3d::image_rtm_3d(const std::vector<axis> &axes) {
   image = new hypercube_float(axes);
 }
 
+image_rtm_3d::image_rtm_3d(const char *, const vel_fd_3d *vel) {
+  if (!vel || vel->axes.size() != 3) throw std::runtime_error("image_rtm_3d: needs a 3-D velocity");
+  image = new hypercube_float(vel->axes);
+  image->zero();
+}
+
+// ------------------------------------------------------------------ inputs of the
+// reference's rtm_zero_op constructor
+int param_func::get_int(const char *arg, int def) const {
+  auto it = vals.find(arg ? arg : "");
+  return it == vals.end() ? def : (int)it->second;
+}
+
+float param_func::get_float(const char *arg, float def) const {
+  auto it = vals.find(arg ? arg : "");
+  return it == vals.end() ? def : (float)it->second;
+}
+
+param_func &param_func::set(const std::string &name, double value) {
+  vals[name] = value;
+  return *this;
+}
+
+vel_fd_3d::vel_fd_3d(const std::vector<axis> &ax, const float *vel) : axes(ax) {
+  if (ax.size() != 3 || !vel) throw std::runtime_error("vel_fd_3d: needs three axes and values");
+  vals.assign(vel, vel + (size_t)ax[0].n * ax[1].n * ax[2].n);
+}
+
+float vel_fd_3d::max_vel() const {
+  float m = vals.empty() ? 0.f : vals[0];
+  for (float v : vals) m = std::max(m, v);
+  return m;
+}
+
+float vel_fd_3d::min_vel() const {
+  float m = vals.empty() ? 0.f : vals[0];
+  for (float v : vals) m = std::min(m, v);
+  return m;
+}
+
+float vel_fd_3d::get_min_samp() const {
+  const float dx = axes[0].d, dy = axes[1].d, dz = axes[2].d;
+  if (dz < dx && dz < dy) return dz;
+  if (dy < dx) return dz;
+  return dx;
+}
+
+float vel_fd_3d::get_max_samp() const {
+  const float dx = axes[0].d, dy = axes[1].d, dz = axes[2].d;
+  if (dz > dx && dz > dy) return dz;
+  if (dy > dx) return dz;
+  return dx;
+}
+
+source_func::source_func(axis t, const float *w) : at(t) {
+  if (!w || t.n < 1) throw std::runtime_error("source_func: empty wavelet");
+  wavelet.assign(w, w + t.n);
+}
+
+void source_func::set_sources_3d(float s_z, axis a_sx, axis a_sy) {
+  for (int i2 = 0; i2 < a_sy.n; i2++)
+    for (int i1 = 0; i1 < a_sx.n; i1++) {
+      sz.push_back(s_z);
+      sx.push_back(a_sx.o + a_sx.d * i1);
+      sy.push_back(a_sy.o + a_sy.d * i2);
+    }
+}
+
 image_rtm_3d::~image_rtm_3d() {
   delete image;
   delete mute;
@@ -831,6 +973,10 @@ void image_rtm_3d::write_volume() {
 
 data_rtm_3d::data_rtm_3d(const std::vector<axis> &ax) : hypercube_float(ax) {
   if (ax.size() < 3) throw std::runtime_error("data_rtm_3d: needs (t, x, y[, shots]) axes");
+}
+
+data_rtm_3d::data_rtm_3d(const std::vector<axis> &ax, const param_func *par) : data_rtm_3d(ax) {
+  sz = par ? par->get_float("rec_depth", 0.f) : 0.f;
 }
 
 int data_rtm_3d::nshots() const {

@@ -993,6 +993,8 @@ int prop_batch_occupancy(int mode, int stages) {
   return 0;
 }
 
+#include "sepx_prop2.inc"
+
 size_t prop_smem_bytes(int mode) {
   switch (mode) {
     case kSrcProp: return smem_bytes_of<kSrcProp, SEPX_SP_STAGES>();

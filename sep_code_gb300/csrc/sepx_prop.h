@@ -96,6 +96,19 @@ struct alignas(64) PropParams {
   int inj_stride;             // batched launches: injection values per step (points)
 };
 
+// Tensor maps of the two-row tile (32 x 32 cells per CTA, two rows per
+// consumer thread): 40 x 40 halo boxes of the current fields and of
+// v^2 dt^2.  Centre boxes of that tile are two 32 x 16 boxes of the
+// ordinary maps.
+constexpr int kTY2 = 2 * kTY;                 // 32
+constexpr int kHY2 = kTY2 + 2 * kHalo;        // 40
+constexpr int kCenter2 = kTX * kTY2;          // 1024 floats
+constexpr int kHalo2 = kHX * kHY2;            // 1600 floats
+struct alignas(64) Rows2Maps {
+  CUtensorMap cur_h[2];
+  CUtensorMap vel_h;
+};
+
 // Parameter sets of up to kMaxMulti grids (shots) advanced by one launch:
 // CTA b is tile b of the concatenated tile lists (tile_base: prefix sums;
 // tiles of a grid numbered x fastest, then y, then z-chunk).  Held in the

@@ -15,7 +15,7 @@ __all__ = [
     "transfer_source_func", "transfer_receiver_func", "transfer_vel_func1", "transfer_vel_func2",
     "source_prop", "rtm_forward", "rtm_adjoint", "kernel_launches", "device_error", "set_zchunk",
     "sinc_table", "glibc_rand", "rand_subspace", "compute_size", "wavelet_deriv", "source_func",
-    "calc_stability", "receiver_map", "synchronize", "reset",
+    "calc_stability", "receiver_map", "synchronize", "reset", "set_tile_rows",
 ]
 
 
@@ -174,6 +174,12 @@ def device_error() -> int:
 
 def set_zchunk(planes: int) -> None:
     check(lib.sepx_set_zchunk(planes), "set_zchunk")
+
+
+def set_tile_rows(mode: int, rows: int) -> None:
+    """Rows per consumer thread of a step kernel: mode 0 source_prop, 1 Born
+    forward, 2 RTM adjoint; rows 1 (32 x 16 tile) or 2 (32 x 32 tile)."""
+    check(lib.sepx_set_tile_rows(mode, rows), "set_tile_rows")
 
 
 def reset() -> None:

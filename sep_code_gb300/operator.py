@@ -22,6 +22,7 @@ class RtmProblem(C.Structure):
         ("nshots", C.c_int), ("shot_xyz", C.c_void_p),
         ("nbound", C.c_int), ("bc_a", C.c_float), ("bc_b", C.c_float),
         ("mode", C.c_int), ("snap_js", C.c_int), ("snap_prec", C.c_int),
+        ("mo1", C.c_float), ("mo2", C.c_float), ("mo3", C.c_float),
     ]
 
 

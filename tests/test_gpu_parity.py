@@ -126,3 +126,43 @@ def test_errors_are_reported():
     with pytest.raises(gf.SepxError, match="outside the propagated interior"):
         gf.transfer_source_func(bad, np.zeros((9, 10), np.float32))
     assert gf.device_error() == 0
+
+
+@pytest.mark.parametrize("rows", [1, 2])
+@pytest.mark.parametrize("case", [
+    dict(m1=37, m2=23, m3=21, nt=40, seed=11),
+    # y interior 48 cells (padded n2 = 64): one and a half 32-row tiles
+    dict(m1=24, m2=40, m3=20, nt=30, seed=13),
+    dict(m1=20, m2=20, m3=20, nt=30, seed=3, data_dt=0.004, dtw=0.004),
+], ids=["ragged", "halfy", "jt2"])
+def test_tile_rows_parity(rows, case, oracle):
+    """source_prop, Born forward and RTM adjoint with every step kernel on
+    one row (32 x 16 tile) or two rows (32 x 32 tile) per thread: both equal
+    the oracle bit for bit."""
+    s = M.small_survey(**case)
+    st = M.prepare_shot(s)
+    gf.setup_cuda(1)
+    try:
+        for mode in (0, 1, 2):
+            gf.set_tile_rows(mode, rows)
+        g, o = GpuShot(s, st), OracleShot(oracle, s, st)
+        g0, g1 = g.source_prop()
+        o0, o1 = o.source_prop()
+        assert np.array_equal(g0, o0) and np.array_equal(g1, o1)
+        rng = np.random.default_rng(5)
+        rec0 = rng.standard_normal((st.rnx * st.rny, st.nt_big)).astype(np.float32) * 1e-3
+        assert np.array_equal(g.rtm_forward(st.img_lap, rec_init=rec0),
+                              o.rtm_forward(st.img_lap, rec_init=rec0))
+        traces = rng.standard_normal((st.rnx * st.rny, st.nt_big)).astype(np.float32)
+        assert np.array_equal(g.rtm_adjoint(o1, o0, traces), o.rtm_adjoint(o1, o0, traces))
+    finally:
+        for mode in (0, 1, 2):
+            gf.set_tile_rows(mode, 1)
+
+
+def test_tile_rows_rejects_other_modes():
+    gf.setup_cuda(1)
+    with pytest.raises(gf.SepxError):
+        gf.set_tile_rows(3, 2)
+    with pytest.raises(gf.SepxError):
+        gf.set_tile_rows(1, 3)

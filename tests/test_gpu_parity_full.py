@@ -4,7 +4,8 @@
   steps, 128 x 128 surface receivers): ``source_prop`` (both returned
   fields), ``rtm_forward`` (traces) and ``rtm_adjoint`` (image).
 * A 100-step window of the same three loops on the 512 x 512 x 400 layered
-  model (padded 560 x 560 x 496, 262,144 receivers).
+  model (padded 560 x 560 x 496, 262,144 receivers), with a random
+  reflectivity (100 steps reach no interface of the model and back).
 
 Each side prepares its inputs with its own set-up code: the GPU side with the
 product's host math (``sep_code_gb300.model.prepare_shot``), the oracle side
@@ -88,6 +89,11 @@ def test_anomaly_128_full_loops(anomaly):
 
 def test_layered_full_grid_100_steps(oracle):
     s = S.layered_survey(nt=100)
+    # 100 steps reach no interface of the layered model and back: a seeded
+    # random reflectivity everywhere makes the Born traces and the image
+    # non-zero within the window
+    rng = np.random.default_rng(20261206)
+    s.refl = (0.01 * rng.standard_normal(s.refl.shape)).astype(np.float32)
     ref = _oracle_loops(oracle, s)
     st = M.prepare_shot(s, with_image=False)
     assert st.n == (560, 560, 496) and st.nt == 100
