@@ -441,6 +441,8 @@ def run_batch(args):
     out["autotune"] = {"zchunk": z, "stages": st_, "style": ["all-tiles", "persistent"][sty],
                        "ms_per_step": round(ms, 4)}
     res = {}
+    clocks = ClockSampler()
+    clocks.start()
     for how in ("sequential", "persistent", "graph", "graph"):
         b.set_images()   # the previous adjoint wrote its image into the forward's input
         torch.cuda.synchronize()
@@ -459,6 +461,7 @@ def run_batch(args):
         res[key] = {"seconds": round(sec, 4), "gcells": round(updates / sec / 1e9, 2),
                     "loop_seconds": {k: round(evs[i].elapsed_time(evs[i + 1]) / 1e3, 4)
                                      for i, k in enumerate(loops)}}
+    out["clocks"] = clocks.stop()
     b.close()
     out["runs"] = res
     out["value"] = res["graph_replay"]["gcells"]

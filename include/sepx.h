@@ -130,7 +130,10 @@ int sepx_dot_f32(const float *a, const float *b, long long n, double *result);
  * at most sepx_dot_f32_noalloc_max_elems() (268,435,456) elements, larger
  * calls are rejected.  All calls share that array; calls that overlap on the
  * GPU race on it.  The first call on a device looks up the array's address
- * with that device current and should come before any stream capture. */
+ * with that device current and should come before any stream capture; the
+ * address is kept for the device's primary context, so the function assumes
+ * that context (no cudaDeviceReset after the first call, no other context on
+ * the same device).  NULL b sums a; n = 0 writes 0 to d_result. */
 int sepx_dot_f32_noalloc(const float *a, const float *b, long long n, double *d_result,
                          void *stream);
 long long sepx_dot_f32_noalloc_max_elems(void);

@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/sepx.h"
 #include "sepx_common.h"
 
@@ -36,7 +38,12 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_dot_scratch[kMaxBlocks];
 
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+// The array's device address, looked up once per device.  Entries are
+// atomic: two host threads making the first call on one device at the same
+// time both look it up and store the same value.  The address belongs to the
+// device's primary context: after cudaDeviceReset, or from another context
+// on the same device, it is not valid (stated in include/sepx.h).
+std::atomic<double *> g_scratch_addr[kMaxDevices] = {};
 
 __device__ __forceinline__ double block_sum_na(double v) {
   __shared__ double red[kThreadsNA / 32];
@@ -91,17 +98,17 @@ extern "C" int sepx_dot_f32_noalloc(const float *a, const float *b, long long n,
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error("sepx_dot_f32_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return set_error("sepx_dot_f32_noalloc: device %d out of range", dev);
-  if (!g_scratch_addr[dev]) {   // once per device, with that device current
-    double *p = nullptr;
-    e = cudaGetSymbolAddress((void **)&p, g_dot_scratch);
-    if (e != cudaSuccess || !p)
+  double *scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!scratch) {   // once per device, with that device current
+    e = cudaGetSymbolAddress((void **)&scratch, g_dot_scratch);
+    if (e != cudaSuccess || !scratch)
       return set_error("sepx_dot_f32_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_scratch_addr[dev] = p;
+    g_scratch_addr[dev].store(scratch, std::memory_order_release);
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nb = (int)((n + kChunk - 1) / kChunk);
-  if (nb > 0) noalloc_dot_partial<<<nb, kThreadsNA, 0, st>>>(a, b, n, g_scratch_addr[dev]);
-  noalloc_dot_final<<<1, kThreadsNA, 0, st>>>(g_scratch_addr[dev], nb, d_result);
+  if (nb > 0) noalloc_dot_partial<<<nb, kThreadsNA, 0, st>>>(a, b, n, scratch);
+  noalloc_dot_final<<<1, kThreadsNA, 0, st>>>(scratch, nb, d_result);
   e = cudaGetLastError();
   if (e != cudaSuccess) return set_error("sepx_dot_f32_noalloc: launch: %s", cudaGetErrorString(e));
   return 0;

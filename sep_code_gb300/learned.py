@@ -220,11 +220,18 @@ def lsrtm_survey(n: int = 384, nt: int = 3000, nshots: int = 4, d: float = 12.5,
 
 def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 4,
                   snap_prec: str = "bf16", fallback_ratio: float = 0.9, verbose: bool = False,
-                  policies=("fallback",), probe_every: int = 8, target: float = 0.0) -> dict:
+                  policies=("fallback",), probe_every: int = 8, target: float = 0.0,
+                  plain_to_learned: bool = False, plain_cap: int = 200) -> dict:
     """Plain simple_solver + cgstep against the same solver with the learned
     direction (one run per direction policy), on data d = L m_true of the
     survey's reflectivity.  target > 0 stops every run at that relative data
-    residual (niter caps it).  "learned" holds the first policy's run."""
+    residual (niter caps it).  "learned" holds the first policy's run.
+
+    plain_to_learned: plain CG runs after the learned one, until it reaches the
+    learned run's final residual (at most plain_cap iterations), so that both
+    are compared at the same data residual: wall time to it, and each image
+    against the plain image at that residual and against the true
+    reflectivity (key "same_residual")."""
     op = RtmOperator(s, mode="linear", snap_js=snap_js, snap_prec=snap_prec)
     runs = {}
     try:
@@ -232,9 +239,10 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
         d = op.forward(s.refl)
         t_fwd = time.perf_counter() - t0
         dd = float(np.dot(d.astype(np.float64).ravel(), d.astype(np.float64).ravel()))
-        m_plain, r_plain, s_plain = op.lsrtm(d, niter, target=target)
-        if verbose:
-            print("plain", np.sqrt(r_plain / dd), s_plain, flush=True)
+        if not plain_to_learned:
+            m_plain, r_plain, s_plain = op.lsrtm(d, niter, target=target)
+            if verbose:
+                print("plain", np.sqrt(r_plain / dd), s_plain, flush=True)
         net = load_network() if net is None else net
         for pol in policies:
             hook = UNetDirection(net, op.model_shape)
@@ -245,6 +253,11 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
                          None if used is None else used.tolist())
             if verbose:
                 print("learned", pol, np.sqrt(r_nn / dd), s_nn, flush=True)
+        if plain_to_learned:
+            r_goal = float(np.sqrt(runs[policies[0]][1][-1] / dd)) * (1 + 1e-9)
+            m_plain, r_plain, s_plain = op.lsrtm(d, plain_cap, target=r_goal)
+            if verbose:
+                print("plain", np.sqrt(r_plain / dd), s_plain, flush=True)
     finally:
         op.close()
 
@@ -276,8 +289,18 @@ def lsrtm_compare(s, niter: int = 20, net: UNet3D | None = None, snap_js: int = 
     def pick(key):
         return first[key] if first else None
 
+    same = None
+    if plain_to_learned and first:
+        m_nn = runs[policies[0]][0]
+        reached = bool(rp[-1] <= first["rel_residual"][-1] * (1 + 1e-9))
+        same = {"residual": first["rel_residual"][-1], "plain_reached": reached,
+                "plain_iterations": len(rp), "plain_seconds": float(s_plain[-1]),
+                "learned_iterations": len(first["rel_residual"]), "learned_seconds": first["seconds"][-1],
+                "speedup": float(s_plain[-1]) / first["seconds"][-1] if reached else None,
+                "image_rel_l2_learned_vs_plain": rel(m_nn, m_plain),
+                "image_rel_l2_vs_true": {"plain": rel(m_plain, s.refl), "learned": rel(m_nn, s.refl)}}
     return {
-        "workload": s.name, "iterations": niter, "target": target or None,
+        "workload": s.name, "iterations": niter, "target": target or None, "same_residual": same,
         "store": f"{snap_prec} every {snap_js} steps",
         "seconds_data_generation": t_fwd,
         "plain": {"rel_residual": rp.tolist(), "seconds": s_plain.tolist()},
@@ -317,6 +340,9 @@ def main(argv=None):
                    help="comma list of fallback,adaptive (empty: plain CG only)")
     c.add_argument("--probe-every", type=int, default=8)
     c.add_argument("--target", type=float, default=0.0)
+    c.add_argument("--plain-to-learned", action="store_true",
+                   help="run plain CG until it reaches the learned run's final residual")
+    c.add_argument("--plain-cap", type=int, default=200)
     a = p.parse_args(argv)
     if a.cmd == "train":
         t0 = time.perf_counter()
@@ -334,7 +360,7 @@ def main(argv=None):
         s = lsrtm_survey(a.n, a.nt, a.shots)
         res = lsrtm_compare(s, a.iters, net=load_network(a.weights), verbose=True,
                             policies=tuple(x for x in a.policies.split(",") if x), probe_every=a.probe_every,
-                            target=a.target)
+                            target=a.target, plain_to_learned=a.plain_to_learned, plain_cap=a.plain_cap)
         txt = json.dumps(res)
         print(txt)
         if a.out:

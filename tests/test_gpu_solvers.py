@@ -11,8 +11,12 @@ vectors) against the reference and against FP64 least squares.
   model is the FP64 least-squares solution (relative L2 1e-5).
 * prec_solver ([L P; eps I], model P x, Born/lin_solver.cpp:21-38) and
   reg_solver ([L; eps R], :39-53, with the scaled identity i_op and with a
-  dense R) against the FP64 solutions of their normal equations (relative
-  L2 1e-5 after 40 iterations: float vectors, well-conditioned problems).
+  dense R) against the FP64 solutions of their normal equations, after 40
+  iterations: the objective |L m - d|^2 + |eps R m|^2 within 1e-7 of its
+  minimum (relative), the model within 1e-3 relative L2.  Float vectors set
+  the floor: the recursively updated residual reaches the minimum to ~1e-8
+  while the model stops 1e-4 to 1e-7 from the FP64 solution, depending on
+  rounding (measured 1.3e-4 for the identity regulariser).
   The reference's own prec_solver and reg_solver cannot pin these: compiled
   here and run on the same dense problem they end in a segmentation fault.
 * row_op (B A) and col_op ([A; C], Born/combo_oper.cpp) forward, adjoint and
@@ -90,26 +94,52 @@ def test_cgstep_matches_reference(run):
     assert _rel(models[-1], SO.lstsq(inp["A"], inp["d"])) <= 1e-5
 
 
+def _objective(A, m, d, R=None, eps=0.0, x=None):
+    A = np.asarray(A, np.float64)
+    m = np.asarray(m, np.float64)
+    r = A @ m - np.asarray(d, np.float64)
+    reg = eps * (np.asarray(R, np.float64) @ (m if x is None else x))
+    return float(r @ r + reg @ reg)
+
+
 def test_prec_solver_lstsq(run):
     inp, _, out, (_, eps) = run
-    want = SO.prec_lstsq(inp["A"], inp["P"], float(np.float32(eps)), inp["d"])
-    assert _rel(out("prec_model"), want) <= 1e-5
+    e = float(np.float32(eps))
+    want = SO.prec_lstsq(inp["A"], inp["P"], e, inp["d"])
+    got = out("prec_model")
+    nc = inp["A"].shape[1]
+    P = inp["P"].astype(np.float64)
+    f_got = _objective(inp["A"], got, inp["d"], np.eye(nc), e, x=np.linalg.solve(P, got))
+    f_min = _objective(inp["A"], want, inp["d"], np.eye(nc), e, x=np.linalg.solve(P, want))
+    assert f_got - f_min <= 1e-7 * f_min
+    assert _rel(got, want) <= 1e-3
 
 
 def test_reg_solver_identity_lstsq(run):
     inp, _, out, (_, eps) = run
+    e = float(np.float32(eps))
     nc = inp["A"].shape[1]
-    want = SO.reg_lstsq(inp["A"], np.eye(nc), float(np.float32(eps)), inp["d"])
+    want = SO.reg_lstsq(inp["A"], np.eye(nc), e, inp["d"])
+    got = out("reg_i_model")
     for name in ("prec", "reg_i", "reg_r"):
         r = out(f"{name}_resid", np.float64)
         print(f"SOLVER {name}: {len(r)} iterations, rr.rr {r[0]:.6e} -> {r[-1]:.10e}")
-    assert _rel(out("reg_i_model"), want) <= 1e-5
+    f_got = _objective(inp["A"], got, inp["d"], np.eye(nc), e)
+    f_min = _objective(inp["A"], want, inp["d"], np.eye(nc), e)
+    print(f"SOLVER reg_i objective above minimum {(f_got - f_min) / f_min:.2e}, model {_rel(got, want):.2e}")
+    assert f_got - f_min <= 1e-7 * f_min
+    assert _rel(got, want) <= 1e-3
 
 
 def test_reg_solver_dense_lstsq(run):
     inp, _, out, (_, eps) = run
-    want = SO.reg_lstsq(inp["A"], inp["R"], float(np.float32(eps)), inp["d"])
-    assert _rel(out("reg_r_model"), want) <= 1e-5
+    e = float(np.float32(eps))
+    want = SO.reg_lstsq(inp["A"], inp["R"], e, inp["d"])
+    got = out("reg_r_model")
+    f_got = _objective(inp["A"], got, inp["d"], inp["R"], e)
+    f_min = _objective(inp["A"], want, inp["d"], inp["R"], e)
+    assert f_got - f_min <= 1e-7 * f_min
+    assert _rel(got, want) <= 1e-3
 
 
 def test_row_col_ops(run):
