@@ -49,6 +49,7 @@ struct PointMapDev {
   int *next = nullptr;        // [npts]
   long long *off = nullptr;   // [npts] pitched offsets from the origin
   int nslot = 0;
+  std::vector<int> built;     // the points the maps were built from
 };
 
 struct Ctx {
@@ -273,6 +274,11 @@ bool inside_interior(int loc, int *x, int *y, int *z) {
 // Plane-indexed point maps: the kernel checks one slot per z plane and chains
 // points that share a cell in ascending id order.
 int build_pointmap(PointMapDev &m, const std::vector<int> &loc, int npts, const char *what) {
+  // the same points again (a shot's receivers transferred once per loop):
+  // the maps on the device are still right
+  if (m.npts == npts && m.plane_slot && (int)m.built.size() == npts &&
+      std::equal(m.built.begin(), m.built.end(), loc.begin()))
+    return 0;
   free_pointmap(m);
   std::vector<int> slot(G.n3, -1), next(std::max(npts, 1), -1);
   std::vector<long long> off(std::max(npts, 1), 0);
@@ -305,6 +311,7 @@ int build_pointmap(PointMapDev &m, const std::vector<int> &loc, int npts, const 
   CK(cudaMemcpyAsync(m.next, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice, G.stream));
   CK(cudaMemcpyAsync(m.off, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice, G.stream));
   CK(cudaStreamSynchronize(G.stream));   // host vectors go out of scope
+  m.built.assign(loc.begin(), loc.begin() + npts);
   return 0;
 }
 

@@ -435,7 +435,31 @@ def main(argv=None):
     p.add_argument("--n", type=int, default=64)
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--gather", action="store_true", help="use the per-tap gather kernel")
+    p.add_argument("--train-steps", type=int, default=0,
+                   help="instead: time this many Adam training steps on a batch of nb x n^3")
     a = p.parse_args(argv)
+    if a.train_steps > 0:
+        import torch
+        model = UNet3D(seed=3)
+        g = torch.Generator(device="cuda").manual_seed(9)
+        x = torch.randn(a.nb, a.n, a.n, a.n, device="cuda", generator=g)
+        t = torch.randn(a.nb, a.n, a.n, a.n, device="cuda", generator=g)
+        torch.cuda.synchronize()
+        model.train_step(x, t)
+        s = model.stream
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(s)
+        for _ in range(a.train_steps):
+            model.zero_grad()
+            model.forward_device(x)
+            model.loss_grad(t)
+            model.backward_device()
+            model.adam_step(1e-3)
+        ev[1].record(s)
+        ev[1].synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / a.train_steps
+        print(f"train step on {a.nb} x {a.n}^3: {ms:.3f} ms")
+        return
     for spec in a.layers.split(","):
         cin, cout = (int(v) for v in spec.split(":"))
         ms = conv_layer_timing(cin, cout, a.nb, a.n, a.reps, halo=not a.gather)
