@@ -1,3 +1,5 @@
+#include <algorithm>
+#include <cstdint>
 // sepx_aux.cu -- small kernels around the fused propagation step: per-step
 // source injection values, the adjoint's injection into the current source
 // field, trace layout transposes, and helpers for the trace/image operators.
@@ -81,6 +83,41 @@ cudaError_t launch_point_add(float *p, const long long *off, const float *inj, i
                              cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;
   point_add_kernel<<<1, 32, 0, st>>>(p, off, inj, npts);
+  return cudaGetLastError();
+}
+
+// rows of `width` floats from one row pitch to another (a dense host-layout
+// volume into the pitched device layout and back); 16-byte accesses where
+// both pitches and both bases allow them
+__global__ void repitch_kernel(const float *__restrict__ src, long long spitch, float *__restrict__ dst,
+                               long long dpitch, int width, long long rows, int vec4) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (vec4) {
+    const int w4 = width >> 2;
+    const long long n = rows * w4;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+      const long long r = i / w4, c = i - r * w4;
+      const float4 v = __ldcs(reinterpret_cast<const float4 *>(src + r * spitch) + c);
+      __stcs(reinterpret_cast<float4 *>(dst + r * dpitch) + c, v);
+    }
+  } else {
+    const long long n = rows * width;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+      const long long r = i / width, c = i - r * width;
+      dst[r * dpitch + c] = __ldcs(src + r * spitch + c);
+    }
+  }
+}
+
+cudaError_t launch_repitch(const float *src, long long spitch, float *dst, long long dpitch,
+                           int width, long long rows, cudaStream_t st) {
+  if (width <= 0 || rows <= 0) return cudaSuccess;
+  const int vec4 = (width % 4 == 0 && spitch % 4 == 0 && dpitch % 4 == 0 &&
+                    reinterpret_cast<uintptr_t>(src) % 16 == 0 && reinterpret_cast<uintptr_t>(dst) % 16 == 0);
+  const long long work = rows * (vec4 ? width / 4 : width);
+  const long long blocks = std::min<long long>((work + 255) / 256, 152LL * 16);
+  repitch_kernel<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, st>>>(src, spitch, dst, dpitch, width,
+                                                                           rows, vec4);
   return cudaGetLastError();
 }
 

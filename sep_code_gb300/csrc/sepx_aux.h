@@ -36,6 +36,9 @@ struct PointAddSets {
 cudaError_t launch_point_add_multi(const PointAddSets &sets, cudaStream_t st);
 cudaError_t launch_transpose(const float *in, long long lda, float *out, long long ldb, int rows,
                              int cols, cudaStream_t st);
+// rows of `width` floats from row pitch spitch to row pitch dpitch (floats)
+cudaError_t launch_repitch(const float *src, long long spitch, float *dst, long long dpitch,
+                           int width, long long rows, cudaStream_t st);
 
 cudaError_t launch_img_from_model(const float *model, int m1, int m2, int m3, int f1, int f2, int f3,
                                   float *img, int n1, int n2, int n3, int pitch, cudaStream_t st);

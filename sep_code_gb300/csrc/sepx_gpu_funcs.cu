@@ -226,10 +226,11 @@ int zero_volume(Volume &v) {
   return 0;
 }
 
-// Host volumes are dense (n1 floats per row), device volumes pitched: a
-// pitched host-to-device copy runs at about a third of the link's speed on
-// GB300, so whole planes go over as flat copies into the staging buffer and
-// are re-pitched device to device.
+// Host volumes are dense (n1 floats per row), device volumes pitched.  A
+// pitched copy (cudaMemcpy2D) moves rows of n1 floats one by one and runs far
+// below the link's rate on GB300 (24-50 GB/s for 2240-byte rows against
+// 191-208 GB/s for flat copies), so whole planes go over as flat copies
+// through the staging buffer and a kernel re-pitches them on the device.
 int h2d_volume(Volume &v, const float *host) {
   const size_t plane = (size_t)G.n1 * G.n2;
   const size_t nz = std::max<size_t>(1, ((size_t)64 << 20) / (plane * 4));
@@ -237,15 +238,22 @@ int h2d_volume(Volume &v, const float *host) {
   for (size_t z0 = 0; z0 < (size_t)G.n3; z0 += nz) {
     const size_t k = std::min(nz, (size_t)G.n3 - z0);
     CK(cudaMemcpyAsync(G.d_stage, host + z0 * plane, k * plane * 4, cudaMemcpyHostToDevice, G.stream));
-    CK(cudaMemcpy2DAsync(v.origin + z0 * G.plane, (size_t)G.pitch * 4, G.d_stage, (size_t)G.n1 * 4,
-                         (size_t)G.n1 * 4, k * G.n2, cudaMemcpyDeviceToDevice, G.stream));
+    CKL(launch_repitch(G.d_stage, G.n1, v.origin + z0 * G.plane, G.pitch, G.n1, (long long)k * G.n2,
+                       G.stream));
   }
   return 0;
 }
 
 int d2h_volume(float *host, const Volume &v) {
-  CK(cudaMemcpy2DAsync(host, (size_t)G.n1 * 4, v.origin, (size_t)G.pitch * 4, (size_t)G.n1 * 4,
-                       (size_t)G.n2 * G.n3, cudaMemcpyDeviceToHost, G.stream));
+  const size_t plane = (size_t)G.n1 * G.n2;
+  const size_t nz = std::max<size_t>(1, ((size_t)64 << 20) / (plane * 4));
+  RET(ensure(&G.d_stage, &G.stage_cap, std::min<size_t>(nz, G.n3) * plane));
+  for (size_t z0 = 0; z0 < (size_t)G.n3; z0 += nz) {
+    const size_t k = std::min(nz, (size_t)G.n3 - z0);
+    CKL(launch_repitch(v.origin + z0 * G.plane, G.pitch, G.d_stage, G.n1, G.n1, (long long)k * G.n2,
+                       G.stream));
+    CK(cudaMemcpyAsync(host + z0 * plane, G.d_stage, k * plane * 4, cudaMemcpyDeviceToHost, G.stream));
+  }
   return 0;
 }
 
@@ -813,6 +821,9 @@ int sepx_transfer_source_func(int npts, int nt, const int *locs, const float *va
     CK(cudaMemcpyAsync(G.d_src_vals, vals, sizeof(float) * (size_t)npts * nt, cudaMemcpyHostToDevice,
                        G.stream));
   RET(build_pointmap(G.srcmap, G.src_loc, npts, "source"));
+  // the caller's buffer is read when the call returns (the reference copies
+  // synchronously)
+  CK(cudaStreamSynchronize(G.stream));
   return 0;
 }
 
@@ -833,6 +844,9 @@ int sepx_transfer_receiver_func(int nx, int ny, int nt, const int *locs, const f
   // the reference's 2-D receiver launch reaches receivers i < n1*n2 only
   const int nact = (int)std::min<long long>(nrec, (long long)G.n1 * G.n2);
   RET(build_pointmap(G.recmap, G.rec_loc, nact, "receiver"));
+  // the caller's traces are read when the call returns (the reference copies
+  // synchronously)
+  CK(cudaStreamSynchronize(G.stream));
   return 0;
 }
 
@@ -851,6 +865,9 @@ int sepx_set_receivers(int nx, int ny, int nt, const int *locs) {
   CK(cudaMemsetAsync(G.d_trc, 0, sizeof(float) * (size_t)std::max(nrec, 1) * nt, G.stream));
   const int nact = (int)std::min<long long>(nrec, (long long)G.n1 * G.n2);
   RET(build_pointmap(G.recmap, G.rec_loc, nact, "receiver"));
+  // the caller's traces are read when the call returns (the reference copies
+  // synchronously)
+  CK(cudaStreamSynchronize(G.stream));
   return 0;
 }
 
