@@ -136,6 +136,57 @@ def build_ref(force: bool = False) -> Path | None:
     return REF_SO
 
 
+REF_CUBIN = REF_OUT / "ref_kernels.cubin"
+
+
+def build_ref_kernels(force: bool = False) -> Path | None:
+    """The reference's own GPU kernels (Born/wave_fkernel.3d8o.cu and the five
+    kernels of Born/gpu_funcs_3d.cu) compiled for sm_103a into a cubin, loaded
+    by oracle/ref_gpu.py through the driver API on the GPU.  Only device code
+    is built, so the cubin needs no host toolchain where it runs.
+
+    Mechanical adjustments to the text handed to nvcc (a temporary file; no
+    copy in the repository): the two unused `texture<>` declarations of
+    Born/gpu_finite_3d.h:85-86 are dropped (CUDA 12 removed texture
+    references); one `__syncthreads()` closes the z loop of wave_kernel and
+    wave_kernel_adj (Born/wave_fkernel.3d8o.cu:104, :179: without it a warp
+    can overwrite its rows of the shared tile for the next plane while
+    another warp still reads them); cuda.h is included for cudaErrors.cu; the
+    CUDA 4 SDK helper headers are empty stand-ins (oracle/ref_stubs/cutil_*.h;
+    no kernel uses them).  Flags of the reference's Makefile: -ftz=true,
+    -maxrregcount=32.  Built only where the reference tree is present."""
+    import tempfile
+    born = REF_ROOT / "Born"
+    if not born.is_dir():
+        return REF_CUBIN if REF_CUBIN.exists() else None
+    REF_OUT.mkdir(exist_ok=True)
+    srcs = [born / "gpu_funcs_3d.cu", born / "gpu_finite_3d.h", born / "wave_fkernel.3d8o.cu",
+            born / "cudaErrors.cu", HERE / "ref_stubs" / "cutil_inline.h",
+            HERE / "ref_stubs" / "cutil_math.h", Path(__file__)]
+    if not force and _newer(REF_CUBIN, srcs):
+        return REF_CUBIN
+    fin = "".join(ln for ln in (born / "gpu_finite_3d.h").read_text().splitlines(keepends=True)
+                  if not ln.lstrip().startswith("texture"))
+    wk = (born / "wave_fkernel.3d8o.cu").read_text()
+    if wk.count("addr+=stride;") != 2:
+        raise RuntimeError("unexpected layout of wave_fkernel.3d8o.cu")
+    wk = wk.replace("addr+=stride;", "addr+=stride;\n\t\t__syncthreads();")
+    text = (born / "gpu_funcs_3d.cu").read_text()
+    text = text.replace('#include "gpu_finite_3d.h"', fin).replace('#include "wave_fkernel.3d8o.cu"', wk)
+    text = "#include <cuda.h>\n" + text
+    nvcc = str(Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "bin" / "nvcc")
+    with tempfile.TemporaryDirectory() as td:
+        src = Path(td) / "ref_kernels.cu"
+        src.write_text(text)
+        tmp = str(REF_CUBIN) + ".tmp"
+        subprocess.run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-ftz=true",
+                        "-maxrregcount=32", "-w", f"-I{HERE / 'ref_stubs'}", f"-I{born}", str(src), "-o",
+                        tmp], check=True)
+    os.replace(tmp, REF_CUBIN)
+    return REF_CUBIN
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_kernels(force="--force" in sys.argv))

@@ -1,0 +1,2 @@
+/* Stand-in for the CUDA 4 SDK helper header the reference includes; its GPU
+   kernels use nothing from it (test infrastructure). */
