@@ -36,14 +36,24 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
                        int y_cstride, int y_coff, float *yf, const float *resid, void *stream);
 /* 3x3x3 layers whose planes are at least 16 x 8 voxels and whose packed
  * weights and input halo fit in 227 KB of shared memory run on the
- * halo-staged kernel; enable = 0 sends every layer to the per-tap gather
- * kernel.  Returns the previous setting. */
+ * halo-staged kernel, and the weight gradients of 3x3x3 layers with at most
+ * 40 output and 80 input channels on the TMA-staged tap-stacked kernel;
+ * enable = 0 sends every layer to the per-tap gather kernels.  Returns the
+ * previous setting. */
 int sepx_unet_set_halo(int enable);
 /* dw[t*cin + c][cout] += sum_v x[v + off(t)][c] dy[v][cout]  (FP32
  * accumulation); dy holds cout rounded up to 8 channels at dy_coff */
 int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
                          int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
                          float *dw, void *stream);
+/* The same, plus db[cout] += sum_v dy[v][cout] when db is not NULL (taken
+ * from the same tiles on the tap-stacked kernel).  The tap-stacked kernel
+ * sums per-CTA partials in a fixed order (repeatable results); it keeps them
+ * in a library scratch buffer, so calls on different streams must not
+ * overlap, and the first call of a shape must not be inside a graph capture. */
+int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
+                              int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
+                              float *dw, float *db, void *stream);
 /* 2x2x2 average pooling and its gradient (accumulate 1: dx += ...) */
 int sepx_unet_avgpool(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int c,
                       void *y, int y_cstride, int y_coff, void *stream);
@@ -69,6 +79,22 @@ int sepx_unet_mse(const float *out, const float *target, long long V, void *g, i
 /* Adam step on FP32 parameters (step counts from 1) */
 int sepx_unet_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1,
                    float b2, float eps, int step, void *stream);
+/* The same step with its hyper-parameters read from device memory when the
+ * kernel runs: hp = {lr, b1, b2, eps, step} (FP32; step counts from 1, exact
+ * below 2^24), so that a captured training step replays with the current
+ * learning rate and step count.  A step below 1 makes no update and sets the
+ * status word (sepx_unet_status() == 5). */
+int sepx_unet_adam_dev(float *p, const float *g, float *m, float *v, long long n, const float *hp,
+                       void *stream);
+/* CUDA-graph capture of the calls this thread enqueues on `stream` (not the
+ * legacy stream) between begin and end; end instantiates the graph and
+ * returns its handle, launch replays it on a stream, free releases it.
+ * Nothing may synchronise or allocate between begin and end: run the
+ * captured sequence once without capture first. */
+int sepx_unet_capture_begin(void *stream);
+int sepx_unet_capture_end(void *stream, void **graph);
+int sepx_unet_graph_launch(void *graph, void *stream);
+int sepx_unet_graph_free(void *graph);
 /* device status word of the convolution kernels (0 = no bounded wait gave up) */
 int sepx_unet_status(void);
 

@@ -16,6 +16,7 @@ enum DevErr : int {
   kErrEmptyWait = 2,   // producer gave up waiting for consumers to free a stage
   kErrDrainWait = 3,   // exit-time wait for in-flight copies gave up
   kErrMmaWait = 4,     // wait for tensor-core MMAs to finish gave up
+  kErrAdamStep = 5,    // Adam read a step count below 1 from device memory (no update made)
 };
 
 constexpr unsigned long long kWaitBudgetNs = 2000000000ull;  // 2 s

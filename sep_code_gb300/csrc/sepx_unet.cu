@@ -705,6 +705,8 @@ __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
   if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+#include "sepx_unet_wgrad.inc"
+
 // ---------------------------------------------------------------------------
 // Weight packing.  w: FP32 master weights in the weight-gradient layout
 // [ntap][cin_p][cout] (row m = t*cin_p + c).  Forward operand
@@ -861,19 +863,42 @@ __global__ void relu_mask_kernel(View y, __nv_bfloat16 *dy, int dy_cstride, int 
   }
 }
 
-// column sums of a BF16 gradient view (the bias gradient): db[c] += sum_v dy[v][c]
-__global__ void bias_grad_kernel(View dy, long long V, int c, float *db) {
-  __shared__ float part[kMaxN];
-  for (int i = threadIdx.x; i < c; i += blockDim.x) part[i] = 0.f;
-  __syncthreads();
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < V * c;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int ch = (int)(e % c);
-    const long long v = e / c;
-    atomicAdd(&part[ch], __bfloat162float(dy.p[v * dy.cstride + dy.coff + ch]));
+// column sums of a BF16 gradient view (the bias gradient): db[c] += sum_v dy[v][c].
+// Thread: one 8-channel group (16-byte loads) over a strided set of voxels,
+// sums in registers; the block's partial per channel goes to part[block]
+// and bias_sum_kernel adds the blocks in a fixed order.
+constexpr int kBiasThreads = 256;
+__global__ void __launch_bounds__(kBiasThreads) bias_grad_kernel(View dy, long long V, int c, float *part) {
+  __shared__ float red[kBiasThreads][9];
+  const int ng = (c + 7) / 8;
+  const int lanes = kBiasThreads / ng;   // voxel lanes of the block (ng <= 16)
+  const int g = threadIdx.x % ng, vl = threadIdx.x / ng;
+  float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (vl < lanes) {
+    for (long long v = blockIdx.x * (long long)lanes + vl; v < V; v += (long long)gridDim.x * lanes) {
+      const uint4 q = *reinterpret_cast<const uint4 *>(dy.p + v * dy.cstride + dy.coff + 8 * g);
+      const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+      for (int i = 0; i < 8; i++) s[i] += __bfloat162float(h[i]);
+    }
   }
+#pragma unroll
+  for (int i = 0; i < 8; i++) red[threadIdx.x][i] = s[i];
   __syncthreads();
-  for (int i = threadIdx.x; i < c; i += blockDim.x) atomicAdd(db + i, part[i]);
+  for (int ch = threadIdx.x; ch < c; ch += kBiasThreads) {
+    const int gg = ch / 8, i = ch % 8;
+    float t = 0.f;
+    for (int l = 0; l < lanes; l++) t += red[l * ng + gg][i];
+    part[(size_t)blockIdx.x * c + ch] = t;
+  }
+}
+
+__global__ void bias_sum_kernel(const float *__restrict__ part, int blocks, int c, float *db) {
+  for (int ch = threadIdx.x; ch < c; ch += blockDim.x) {
+    float t = 0.f;
+    for (int b = 0; b < blocks; b++) t += part[(size_t)b * c + ch];
+    db[ch] += t;
+  }
 }
 
 // FP32 volume (one channel) -> BF16 channel-last view channel 0, other
@@ -908,8 +933,22 @@ __global__ void mse_kernel(const float *out, const float *target, long long V, _
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc / (double)V);
 }
 
-__global__ void adam_kernel(float *p, const float *g, float *m, float *v, long long n, float lr,
-                            float b1, float b2, float eps, float c1, float c2) {
+// hp (optional): {lr, b1, b2, eps, step} read when the kernel runs, so that a
+// captured training step replays with the current learning rate and step;
+// the bias corrections are formed here in both forms
+__global__ void adam_kernel(float *p, const float *g, float *m, float *v, long long n,
+                            const float *hp, float lr, float b1, float b2, float eps, int step,
+                            int *err) {
+  if (hp) {
+    lr = hp[0]; b1 = hp[1]; b2 = hp[2]; eps = hp[3];
+    const float s = hp[4];
+    if (!(s >= 1.f)) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(err, 0, (int)kErrAdamStep);
+      return;
+    }
+    step = (int)s;
+  }
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const float gi = g[i];
@@ -969,40 +1008,74 @@ PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
 size_t g_smem_per_sm = 0, g_smem_reserved = 0;
 
+// the tensor-map encoder and the device figures the persistent grids are sized from
+int unet_dev_init() {
+  if (g_encode) return 0;
+  cudaDriverEntryPointQueryResult q;
+  void *fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+      !fn || q != cudaDriverEntryPointSuccess)
+    return set_error("unet conv: cuTensorMapEncodeTiled is unavailable");
+  int dev = 0, smem_sm = 0, resv = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
+    return set_error("unet conv: cannot query the device");
+  g_smem_per_sm = (size_t)smem_sm;
+  g_smem_reserved = (size_t)resv;
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return 0;
+}
+
+// channel-last BF16 view as a 5-D tensor (channels, W, H, D, volumes) with a
+// box of 8 channels x bx x by x bz x 1
+int encode_view(CUtensorMap *tm, const void *p, int cstride, int coff, int chans, int nb, int D, int H,
+                int W, int bx, int by, int bz, const char *what) {
+  const __nv_bfloat16 *base = (const __nv_bfloat16 *)p + coff;
+  if (reinterpret_cast<uintptr_t>(base) % 16) return set_error("unet %s: view not 16-byte aligned", what);
+  const cuuint64_t cs = (cuuint64_t)cstride * 2;
+  cuuint64_t dims[5] = {(cuuint64_t)chans, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)nb};
+  cuuint64_t strides[4] = {cs, cs * W, cs * W * H, cs * W * H * D};
+  cuuint32_t box[5] = {8, (cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(base), dims,
+                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error("unet %s: cuTensorMapEncodeTiled failed (%d)", what, (int)r);
+  return 0;
+}
+
+// Device scratch for partial sums, grown on demand (a call inside a CUDA-graph
+// capture must not grow it: run the sequence once before capturing).
+float *g_scratch = nullptr;
+size_t g_scratch_floats = 0;
+int unet_scratch(size_t floats, float **p) {
+  if (floats > g_scratch_floats) {
+    float *q = nullptr;
+    if (cudaMalloc((void **)&q, floats * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error("unet: cannot allocate %zu floats of scratch", floats);
+    }
+    if (g_scratch) {
+      cudaDeviceSynchronize();   // nothing may still read the old buffer
+      cudaFree(g_scratch);
+    }
+    g_scratch = q;
+    g_scratch_floats = floats;
+  }
+  *p = g_scratch;
+  return 0;
+}
+
 int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
               const void *wpacked, uint32_t wbytes, const float *bias, int cout, int np, int relu,
               void *y, int y_cstride, int y_coff, float *yf, const float *resid, int *err,
               cudaStream_t st) {
-  if (!g_encode) {
-    cudaDriverEntryPointQueryResult q;
-    void *fn = nullptr;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        !fn || q != cudaDriverEntryPointSuccess)
-      return set_error("unet conv: cuTensorMapEncodeTiled is unavailable");
-    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    int dev = 0, smem_sm = 0, resv = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
-      return set_error("unet conv: cannot query the device");
-    g_smem_per_sm = (size_t)smem_sm;
-    g_smem_reserved = (size_t)resv;
-  }
-  // x as a 5-D tensor (channels of the view, W, H, D, volumes), channels innermost
-  const __nv_bfloat16 *base = (const __nv_bfloat16 *)x + x_coff;
-  if (reinterpret_cast<uintptr_t>(base) % 16) return set_error("unet conv: input view not 16-byte aligned");
-  const cuuint64_t cs = (cuuint64_t)x_cstride * 2;
-  cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)nb};
-  cuuint64_t strides[4] = {cs, cs * W, cs * W * H, cs * W * H * D};
-  cuuint32_t box[5] = {8, (cuuint32_t)kHaloX, (cuuint32_t)kHaloY, (cuuint32_t)kHaloZ, 1};
-  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  if (unet_dev_init()) return -1;
   CUtensorMap tm;
-  CUresult r = g_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(base), dims,
-                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return set_error("unet conv: cuTensorMapEncodeTiled failed (%d)", (int)r);
+  if (encode_view(&tm, x, x_cstride, x_coff, cin, nb, D, H, W, kHaloX, kHaloY, kHaloZ, "conv")) return -1;
   HaloArgs a;
   a.nb = nb; a.D = D; a.H = H; a.W = W; a.cin = cin; a.cout = cout; a.np = np; a.relu = relu;
   a.bias = bias; a.y = (__nv_bfloat16 *)y; a.y_cstride = y_cstride; a.y_coff = y_coff;
@@ -1047,6 +1120,100 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
   conv_halo_kernel<<<(unsigned)grid, kHaloThreads, smem, st>>>(tm, (const __nv_bfloat16 *)wpacked, a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
+}
+
+// The tap-stacked TMA weight gradient (sepx_unet_wgrad.inc) for 3x3x3 layers
+// with 3 x (cout rounded to 8) <= 128 rows and 3 x cin / 8 + 1 N groups <= 32.
+// Returns 1 where it does not apply (the caller takes the gather kernel).
+int conv_wgrad_tma(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
+                   const void *dy, int dy_cstride, int dy_coff, int cout, float *dw, float *db, int *err,
+                   cudaStream_t st) {
+  const int ngi = cin / 8, ngo = (cout + 7) / 8;
+  if (!g_halo_enabled || 3 * ngo > 16 || 3 * ngi + 1 > 32) return 1;
+  if (unet_dev_init()) return -1;
+  const int np = ((8 * (3 * ngi + 1)) + 15) / 16 * 16;
+  const uint32_t a_bytes = 3u * ngo * kWgBox;
+  const size_t budget = kHaloMaxSmem - 256 - 128;
+  int ndz = 0, stages = 0;
+  uint32_t stage = 0;
+  auto plan = [&](int nd) {
+    if (nd * np > 512) return 0;
+    const uint32_t sb = a_bytes + (uint32_t)nd * (np / 8) * kWgBox;
+    const size_t slack = sb >= 16u * kWgBox ? 0 : 16u * kWgBox - sb;
+    const size_t k = (budget - slack) / sb;
+    return (int)(k > (size_t)kWgMaxStages ? kWgMaxStages : k);
+  };
+  // three dz per CTA where that still leaves three stages, else one
+  for (int nd : {3, 1}) {
+    const int k = plan(nd);
+    if (k >= 3 || (nd == 1 && k >= 2)) {
+      ndz = nd;
+      stages = k;
+      stage = a_bytes + (uint32_t)nd * (np / 8) * kWgBox;
+      break;
+    }
+  }
+  if (!ndz) return 1;
+  const size_t slack = stage >= 16u * kWgBox ? 0 : 16u * kWgBox - stage;
+  const size_t smem = (size_t)stages * stage + slack + 2 * kWgMaxStages * 8 + 16 + 128;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(conv_wgrad_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kHaloMaxSmem);
+    if (e != cudaSuccess) return set_error("unet wgrad: %s", cudaGetErrorString(e));
+    attr = true;
+  }
+  CUtensorMap tmx, tmy;
+  if (encode_view(&tmx, x, x_cstride, x_coff, cin, nb, D, H, W, 8, 16, 1, "wgrad x") ||
+      encode_view(&tmy, dy, dy_cstride, dy_coff, 8 * ngo, nb, D, H, W, 8, 16, 1, "wgrad dy"))
+    return -1;
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(ndz * np)) ncols <<= 1;
+  int per_sm = (int)(g_smem_per_sm / (((smem + 127) / 128) * 128 + g_smem_reserved));
+  if (per_sm < 1) return 1;
+  if (per_sm * (int)ncols > 512) per_sm = 512 / (int)ncols;
+  const int nzg = 3 / ndz;
+  WgArgs a;
+  a.nb = nb; a.D = D; a.H = H; a.W = W; a.cin = cin; a.cout = cout; a.ngi = ngi; a.ngo = ngo;
+  a.ndz = ndz; a.np = np;
+  a.ty = (H + 15) / 16;
+  a.tx = (W + 2 + 7) / 8;
+  a.ntiles = (long long)nb * D * a.ty * a.tx;
+  a.groups = (g_num_sms * per_sm) / nzg;
+  if (a.groups > a.ntiles) a.groups = (int)a.ntiles;
+  if (a.groups < 1) a.groups = 1;
+  a.stages = stages;
+  a.a_bytes = a_bytes;
+  a.b_bytes = (uint32_t)ndz * (np / 8) * kWgBox;
+  a.stage_bytes = stage;
+  a.err = err;
+  const long long n = 27LL * cin * cout;
+  float *scr;
+  if (unet_scratch((size_t)a.groups * (size_t)(n + cout), &scr)) return -1;
+  a.part = scr;
+  a.bpart = scr + (size_t)a.groups * n;
+  conv_wgrad_tma_kernel<<<(unsigned)(a.groups * nzg), kWgThreads, smem, st>>>(tmx, tmy, a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error("unet wgrad: %s", cudaGetErrorString(e));
+  const long long tot = n + cout;
+  wg_reduce_kernel<<<(unsigned)((tot + 255) / 256 < 1216 ? (tot + 255) / 256 : 1216), 256, 0, st>>>(
+      a.part, a.groups, n, dw, a.bpart, cout, db);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet wgrad: %s", cudaGetErrorString(e));
+}
+
+// db[c] += sum_v dy[v][c]: block partials in the scratch, summed in a fixed order
+int bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V, int c, float *db, cudaStream_t st) {
+  const int ng = (c + 7) / 8;
+  const int lanes = kBiasThreads / ng;
+  long long blocks = (V + lanes - 1) / lanes;
+  if (blocks > 2 * 152) blocks = 2 * 152;
+  float *scr;
+  if (unet_scratch((size_t)blocks * c, &scr)) return -1;
+  View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  bias_grad_kernel<<<(unsigned)blocks, kBiasThreads, 0, st>>>(dv, V, c, scr);
+  bias_sum_kernel<<<1, 128, 0, st>>>(scr, (int)blocks, c, db);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet bias_grad: launch failed");
 }
 }  // namespace
 
@@ -1136,6 +1303,13 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
 int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
                          int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
                          float *dw, void *stream) {
+  return sepx_unet_conv_wgrad_bias(x, x_cstride, x_coff, nb, D, H, W, cin, ntap, dy, dy_cstride, dy_coff,
+                                   cout, dw, nullptr, stream);
+}
+
+int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
+                              int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
+                              float *dw, float *db, void *stream) {
   if (need_dev(x, "wgrad x") || need_dev(dy, "wgrad dy") || need_dev(dw, "wgrad dw") ||
       need_dims(nb, D, H, W, "wgrad"))
     return -1;
@@ -1148,6 +1322,12 @@ int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D
   const long long V = (long long)nb * D * H * W;
   if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
     return set_error("unet wgrad: volume too large (%lld voxels)", V);
+  if (ntap == 27) {
+    const int rc = conv_wgrad_tma(x, x_cstride, x_coff, nb, D, H, W, cin, dy, dy_cstride, dy_coff, cout,
+                                  dw, db, err, (cudaStream_t)stream);
+    if (rc <= 0) return rc;
+  }
+  if (db && bias_grad(dy, dy_cstride, dy_coff, V, cout, db, (cudaStream_t)stream)) return -1;
   const long long vchunks = (V + kKC - 1) / kKC;
   const int mt = (ntap * cin + kTM - 1) / kTM;
   // enough CTAs to fill the GPU about twice, at least 16 voxel chunks each
@@ -1232,9 +1412,9 @@ int sepx_unet_bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V
   if (c > kMaxN || c < 0 || V < 0) return set_error("unet bias_grad: bad shape");
   if (V == 0 || c == 0) return 0;
   if (need_dev(dy, "bias_grad dy") || need_dev(db, "bias_grad db")) return -1;
-  View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
-  bias_grad_kernel<<<grid_for(V * c), 256, 0, (cudaStream_t)stream>>>(dv, V, c, db);
-  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet bias_grad: launch failed");
+  if (dy_cstride % 8 || dy_coff % 8 || dy_coff + ((c + 7) / 8) * 8 > dy_cstride)
+    return set_error("unet bias_grad: bad channel arguments");
+  return bias_grad(dy, dy_cstride, dy_coff, V, c, db, (cudaStream_t)stream);
 }
 
 int sepx_unet_to_bf16(const float *in, long long V, float scale, void *y, int y_cstride, int y_coff,
@@ -1265,9 +1445,63 @@ int sepx_unet_adam(float *p, const float *g, float *m, float *v, long long n, fl
   if (n == 0) return 0;
   if (need_dev(p, "adam p") || need_dev(g, "adam g") || need_dev(m, "adam m") || need_dev(v, "adam v"))
     return -1;
-  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-  adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  int *err;
+  if (unet_err_ptr(&err)) return set_error("unet adam: cannot allocate the status word");
+  adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, nullptr, lr, b1, b2, eps,
+                                                              step, err);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet adam: launch failed");
+}
+
+int sepx_unet_adam_dev(float *p, const float *g, float *m, float *v, long long n, const float *hp,
+                       void *stream) {
+  if (n < 0) return set_error("unet adam: n %lld", n);
+  if (n == 0) return 0;
+  if (need_dev(p, "adam p") || need_dev(g, "adam g") || need_dev(m, "adam m") ||
+      need_dev(v, "adam v") || need_dev(hp, "adam hyper-parameters"))
+    return -1;
+  int *err;
+  if (unet_err_ptr(&err)) return set_error("unet adam: cannot allocate the status word");
+  adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, hp, 0.f, 0.f, 0.f, 0.f, 1,
+                                                              err);
+  return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet adam: launch failed");
+}
+
+int sepx_unet_capture_begin(void *stream) {
+  if (!stream) return set_error("unet capture: the legacy stream cannot be captured");
+  int *err;
+  if (unet_err_ptr(&err)) return set_error("unet capture: cannot allocate the status word");
+  cudaError_t e = cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal);
+  return e == cudaSuccess ? 0 : set_error("unet capture: %s", cudaGetErrorString(e));
+}
+
+int sepx_unet_capture_end(void *stream, void **graph) {
+  if (!stream || !graph) return set_error("unet capture: NULL stream or handle");
+  *graph = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture((cudaStream_t)stream, &g);
+  if (e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return set_error("unet capture: %s", cudaGetErrorString(e != cudaSuccess ? e : cudaErrorUnknown));
+  }
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_error("unet capture: instantiate: %s", cudaGetErrorString(e));
+  *graph = (void *)x;
+  return 0;
+}
+
+int sepx_unet_graph_launch(void *graph, void *stream) {
+  if (!graph) return set_error("unet graph: NULL handle");
+  cudaError_t e = cudaGraphLaunch((cudaGraphExec_t)graph, (cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : set_error("unet graph: %s", cudaGetErrorString(e));
+}
+
+int sepx_unet_graph_free(void *graph) {
+  if (!graph) return 0;
+  cudaError_t e = cudaGraphExecDestroy((cudaGraphExec_t)graph);
+  return e == cudaSuccess ? 0 : set_error("unet graph: %s", cudaGetErrorString(e));
 }
 
 int sepx_unet_status(void) {

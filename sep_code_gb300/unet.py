@@ -40,6 +40,7 @@ _SIGS = {
     "sepx_unet_conv_fwd": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _i, _i, _vp,
                            _vp, _vp],
     "sepx_unet_conv_wgrad": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp, _vp],
+    "sepx_unet_conv_wgrad_bias": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp, _vp, _vp],
     "sepx_unet_avgpool": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _vp],
     "sepx_unet_avgpool_bwd": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp],
     "sepx_unet_upsample": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _vp],
@@ -49,6 +50,11 @@ _SIGS = {
     "sepx_unet_to_bf16": [_vp, _ll, _f, _vp, _i, _i, _vp],
     "sepx_unet_mse": [_vp, _vp, _ll, _vp, _i, _vp, _vp],
     "sepx_unet_adam": [_vp, _vp, _vp, _vp, _ll, _f, _f, _f, _f, _i, _vp],
+    "sepx_unet_adam_dev": [_vp, _vp, _vp, _vp, _ll, _vp, _vp],
+    "sepx_unet_capture_begin": [_vp],
+    "sepx_unet_capture_end": [_vp, C.POINTER(C.c_void_p)],
+    "sepx_unet_graph_launch": [_vp, _vp],
+    "sepx_unet_graph_free": [_vp],
     "sepx_unet_status": [],
     "sepx_unet_set_halo": [_i],
 }
@@ -124,15 +130,28 @@ class UNet3D:
         params = init_params(seed) if params is None else params
         self.w, self.b, self.gw, self.gb, self.mw, self.vw, self.mb, self.vb = ({} for _ in range(8))
         self.pk, self.pkt = {}, {}
+        # parameters, gradients and the two Adam moments each live in one flat
+        # FP32 buffer (per-layer views), so that zeroing the gradients and the
+        # Adam step are one launch each
+        shapes = [(L, (L.ntap, L.cin_p, L.cout), (L.cout,)) for L in LAYERS]
+        total = sum(int(np.prod(ws)) + int(np.prod(bs)) for _, ws, bs in shapes)
         with torch.cuda.stream(self.stream):
-            for L in LAYERS:
+            self.flat = {k: torch.zeros(total, dtype=torch.float32, device=self.dev)
+                         for k in ("p", "g", "m", "v")}
+            # Adam hyper-parameters {lr, b1, b2, eps, step}, read by the kernel
+            self.hp = torch.zeros(5, dtype=torch.float32, device=self.dev)
+            o = 0
+            for L, ws, bs in shapes:
+                nw, nbias = int(np.prod(ws)), int(np.prod(bs))
+                for d, k in ((self.w, "p"), (self.gw, "g"), (self.mw, "m"), (self.vw, "v")):
+                    d[L.name] = self.flat[k][o:o + nw].view(ws)
+                for d, k in ((self.b, "p"), (self.gb, "g"), (self.mb, "m"), (self.vb, "v")):
+                    d[L.name] = self.flat[k][o + nw:o + nw + nbias].view(bs)
+                o += nw + nbias
                 w, b = params[L.name]
-                self.w[L.name] = torch.tensor(np.ascontiguousarray(w, np.float32), device=self.dev)
-                self.b[L.name] = torch.tensor(np.ascontiguousarray(b, np.float32), device=self.dev)
-                for d in (self.gw, self.mw, self.vw):
-                    d[L.name] = torch.zeros_like(self.w[L.name])
-                for d in (self.gb, self.mb, self.vb):
-                    d[L.name] = torch.zeros_like(self.b[L.name])
+                self.w[L.name].copy_(torch.tensor(np.ascontiguousarray(w, np.float32).reshape(ws)))
+                self.b[L.name].copy_(torch.tensor(np.ascontiguousarray(b, np.float32).reshape(bs)))
+            for L in LAYERS:
                 n = lib.sepx_unet_packed_elems(L.cout, L.cin_p, L.ntap, 0)
                 self.pk[L.name] = torch.zeros(n, dtype=torch.bfloat16, device=self.dev)
                 n = lib.sepx_unet_packed_elems(L.cout, L.cin_p, L.ntap, 1)
@@ -140,6 +159,7 @@ class UNet3D:
             self.loss = torch.zeros(1, dtype=torch.float64, device=self.dev)
         self.step_count = 0
         self.shape = None
+        self.graph, self.graph_io = None, None
         self.pack()
 
     # ---------------------------------------------------------------- params
@@ -225,10 +245,9 @@ class UNet3D:
     def _wgrad(self, L, x, xcs, xco, dy, dycs, dyco, lvl):
         nb = self.shape[0]
         D, H, W = self.dims[lvl]
-        _chk(lib.sepx_unet_conv_wgrad(_p(x), xcs, xco, nb, D, H, W, L.cin_p, L.ntap, _p(dy), dycs,
-                                      dyco, L.cout, _p(self.gw[L.name]), self.stream_ptr))
-        _chk(lib.sepx_unet_bias_grad(_p(dy), dycs, dyco, self.V[lvl], L.cout, _p(self.gb[L.name]),
-                                     self.stream_ptr))
+        _chk(lib.sepx_unet_conv_wgrad_bias(_p(x), xcs, xco, nb, D, H, W, L.cin_p, L.ntap, _p(dy), dycs,
+                                           dyco, L.cout, _p(self.gw[L.name]), _p(self.gb[L.name]),
+                                           self.stream_ptr))
 
     def _relu_mask(self, y, ycs, yco, dy, dycs, dyco, lvl, c):
         _chk(lib.sepx_unet_relu_mask(_p(y), ycs, yco, _p(dy), dycs, dyco, self.V[lvl], c,
@@ -360,9 +379,7 @@ class UNet3D:
 
     def zero_grad(self):
         with self.torch.cuda.stream(self.stream):
-            for L in LAYERS:
-                self.gw[L.name].zero_()
-                self.gb[L.name].zero_()
+            self.flat["g"].zero_()
             self.loss.zero_()
 
     def loss_grad(self, target):
@@ -371,27 +388,83 @@ class UNet3D:
         _chk(lib.sepx_unet_mse(_p(self.a["out"]), _p(target), self.V[0], _p(self.g["out"]), 8,
                                _p(self.loss), self.stream_ptr))
 
-    def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+    def _set_hp(self, lr, b1, b2, eps):
+        """next step's Adam hyper-parameters into device memory (ordered on
+        the library stream; the host values are staged before this returns)"""
         self.step_count += 1
-        for L in LAYERS:
-            for p, gr, m, v in ((self.w, self.gw, self.mw, self.vw), (self.b, self.gb, self.mb, self.vb)):
-                _chk(lib.sepx_unet_adam(_p(p[L.name]), _p(gr[L.name]), _p(m[L.name]), _p(v[L.name]),
-                                        p[L.name].numel(), lr, b1, b2, eps, self.step_count,
-                                        self.stream_ptr))
+        hp = self.torch.tensor([lr, b1, b2, eps, float(self.step_count)], dtype=self.torch.float32)
+        with self.torch.cuda.stream(self.stream):
+            self.hp.copy_(hp)
+
+    def _adam_enqueue(self):
+        F = self.flat
+        _chk(lib.sepx_unet_adam_dev(_p(F["p"]), _p(F["g"]), _p(F["m"]), _p(F["v"]), F["p"].numel(),
+                                    _p(self.hp), self.stream_ptr))
+
+    def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self._set_hp(lr, b1, b2, eps)
+        self._adam_enqueue()
         self.pack()
 
-    def train_step(self, x, target, lr=1e-3):
-        """one Adam step on a batch x, target (FP32 device tensors [nb, D, H, W]); returns the loss"""
+    def _step_body(self, x, target):
         self.zero_grad()
         self.forward_device(x)
         self.loss_grad(target)
         self.backward_device()
-        self.adam_step(lr)
+        self._adam_enqueue()
+        self.pack()
+
+    def train_step(self, x, target, lr=1e-3):
+        """one Adam step on a batch x, target (FP32 device tensors [nb, D, H, W]); returns the loss"""
+        self._set_hp(lr, 0.9, 0.999, 1e-8)
+        if self.graph is not None and self.graph_io == (x.data_ptr(), target.data_ptr(), tuple(x.shape)):
+            _chk(lib.sepx_unet_graph_launch(self.graph, self.stream_ptr))
+        else:
+            self._step_body(x, target)
         self.stream.synchronize()
         return float(self.loss.item())
 
+    def capture_train_step(self, x, target):
+        """Capture one whole training step (gradient zeroing, forward, loss,
+        backward, Adam, weight packing: about 140 launches) into a CUDA graph
+        that reads its batch from x and target; train_step on these same
+        tensors then replays it with one launch.  Runs one eager step first
+        (buffer allocation, kernel attributes), which trains the network on
+        this batch once."""
+        self.train_step(x, target)
+        self.free_graph()
+        self.stream.synchronize()
+        _chk(lib.sepx_unet_capture_begin(self.stream_ptr))
+        try:
+            self._step_body(x, target)
+        finally:
+            h = C.c_void_p()
+            rc = lib.sepx_unet_capture_end(self.stream_ptr, C.byref(h))
+        _chk(rc)
+        self.graph = h
+        self.graph_io = (x.data_ptr(), target.data_ptr(), tuple(x.shape))
+
+    def free_graph(self):
+        if self.graph is not None:
+            lib.sepx_unet_graph_free(self.graph)
+        self.graph, self.graph_io = None, None
+
+    def __del__(self):
+        try:
+            self.free_graph()
+        except Exception:
+            pass
+
     def status(self) -> int:
         return lib.sepx_unet_status()
+
+
+_LEVEL = {"e1": 0, "e2": 1, "e3": 2, "b4": 3, "d3": 2, "d2": 1, "d1": 0, "ou": 0}
+
+
+def network_flops(nb: int, n: int) -> float:
+    """multiply-add FLOPs (x2) of one forward pass of every convolution on nb x n^3"""
+    return sum(2.0 * nb * (n >> _LEVEL[L.name[:2]]) ** 3 * L.ntap * L.cin * L.cout for L in LAYERS)
 
 
 def conv_layer_timing(cin: int, cout: int, nb: int = 4, n: int = 64, reps: int = 2, halo: bool = True,
@@ -447,18 +520,30 @@ def main(argv=None):
         torch.cuda.synchronize()
         model.train_step(x, t)
         s = model.stream
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        ev[0].record(s)
-        for _ in range(a.train_steps):
-            model.zero_grad()
-            model.forward_device(x)
-            model.loss_grad(t)
-            model.backward_device()
-            model.adam_step(1e-3)
-        ev[1].record(s)
-        ev[1].synchronize()
-        ms = ev[0].elapsed_time(ev[1]) / a.train_steps
-        print(f"train step on {a.nb} x {a.n}^3: {ms:.3f} ms")
+        flops = 3 * network_flops(a.nb, a.n)   # forward + data gradient + weight gradient
+
+        def timed(step):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record(s)
+            for _ in range(a.train_steps):
+                step()
+            ev[1].record(s)
+            ev[1].synchronize()
+            return ev[0].elapsed_time(ev[1]) / a.train_steps
+
+        def eager():
+            model._set_hp(1e-3, 0.9, 0.999, 1e-8)
+            model._step_body(x, t)
+
+        def replay():
+            model._set_hp(1e-3, 0.9, 0.999, 1e-8)
+            _chk(lib.sepx_unet_graph_launch(model.graph, model.stream_ptr))
+
+        ms = timed(eager)
+        print(f"train step on {a.nb} x {a.n}^3: {ms:.3f} ms ({flops / ms / 1e9:.1f} TFLOP/s), launched one by one")
+        model.capture_train_step(x, t)
+        ms = timed(replay)
+        print(f"train step on {a.nb} x {a.n}^3: {ms:.3f} ms ({flops / ms / 1e9:.1f} TFLOP/s), one graph")
         return
     for spec in a.layers.split(","):
         cin, cout = (int(v) for v in spec.split(":"))

@@ -89,5 +89,17 @@ def test_unet_calls_reject_null_operands(raw):
     _rejects(L, L.sepx_unet_upsample_bwd(None, 8, 0, 1, 4, 8, 8, 8, p, 8, 0, None), "NULL")
     _rejects(L, L.sepx_unet_adam(p, None, p, p, n(8), C.c_float(1e-3), C.c_float(0.9),
                                  C.c_float(0.999), C.c_float(1e-8), 1, None), "NULL")
+    _rejects(L, L.sepx_unet_conv_wgrad_bias(p, 8, 0, 1, 4, 8, 8, 8, 27, None, 8, 0, 8, p, p, None),
+             "NULL")
+    _rejects(L, L.sepx_unet_conv_wgrad_bias(p, 8, 0, 1, 4, 8, 8, 8, 27, p, 8, 0, 8, None, p, None),
+             "NULL")
+    _rejects(L, L.sepx_unet_bias_grad(p, 12, 0, n(4), 8, p, None), "bad channel")
+    _rejects(L, L.sepx_unet_adam_dev(p, p, p, p, n(8), None, None), "NULL")
+    _rejects(L, L.sepx_unet_adam_dev(p, p, p, p, n(-1), p, None), "n -1")
+    assert L.sepx_unet_adam_dev(None, None, None, None, n(0), None, None) == 0
+    _rejects(L, L.sepx_unet_capture_begin(None), "legacy stream")
+    _rejects(L, L.sepx_unet_capture_end(None, None), "NULL")
+    _rejects(L, L.sepx_unet_graph_launch(None, None), "NULL handle")
+    assert L.sepx_unet_graph_free(None) == 0
     _rejects(L, L.sepx_unet_mse(p, p, n(-1), p, 8, p, None), "negative length")
     assert L.sepx_unet_to_bf16(None, n(0), C.c_float(1.0), None, 8, 0, None) == 0

@@ -7,8 +7,10 @@ Tolerances: FP32 outputs of a convolution of BF16 operands differ from the
 FP64 sum only by FP32 accumulation order -- relative L2 <= 1e-5.  Outputs
 stored in BF16 carry its rounding (2^-9 relative): <= 8e-3.  Network
 gradients, where BF16 rounding of every activation can flip near a rounding
-boundary and propagate: within 0.1 of the BF16-storage restatement per layer,
-and no further from the exact FP64 gradient than twice that restatement.
+boundary and propagate: within 0.08 of the BF16-storage restatement per layer
+(measured: at most 0.054, at the 4^3 bottom level, whose sums have fewest
+terms; 0.0006-0.03 elsewhere), and no further from the exact FP64 gradient
+than twice that restatement.
 """
 import numpy as np
 import pytest
@@ -189,7 +191,7 @@ def test_network_gradients_match_oracle(net):
         errs[L.name] = (rel_l2(gw, ew), rel_l2(gb, eb), rel_l2(gw, xw), rel_l2(ew, xw))
     print("UNET_GRAD_REL_L2", errs)
     for name, (ew_, eb_, gx, ox) in errs.items():
-        assert ew_ <= 0.1 and eb_ <= 0.1, (name, ew_, eb_)
+        assert ew_ <= 0.08 and eb_ <= 0.08, (name, ew_, eb_)
         assert gx <= 2.0 * ox + 0.01, (name, gx, ox)
 
 
@@ -208,6 +210,37 @@ def test_training_reduces_loss(net):
     losses = [model.train_step(xt, tt, lr=2e-3) for _ in range(60)]
     assert model.status() == 0
     assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
+
+
+def test_captured_training_step_matches_eager(net):
+    """The whole training step captured once into a CUDA graph and replayed
+    (new learning rate and step count each replay, read from device memory)
+    trains like the same steps launched one by one: same losses and weights
+    to FP32 summation-order noise (some kernels add with atomics)."""
+    rng = np.random.default_rng(8)
+    nb, D, H, W = 2, 16, 16, 32
+    x = rng.standard_normal((nb, D, H, W)).astype(np.float32)
+    t = (0.5 * x + 0.1 * rng.standard_normal(x.shape)).astype(np.float32)
+    xt, tt = torch.tensor(x).cuda(), torch.tensor(t).cuda()
+    lrs = [2e-3, 1.5e-3, 1e-3, 5e-4, 2.5e-4]
+    graph, twin = net.UNet3D(seed=4), net.UNet3D(seed=4)
+    torch.cuda.synchronize()
+    graph.capture_train_step(xt, tt)          # one eager step at lr 1e-3, then the capture
+    assert graph.graph is not None
+    l0 = twin.train_step(xt, tt, lr=1e-3)     # the same first step on the eager twin
+    lg = [graph.train_step(xt, tt, lr=lr) for lr in lrs[1:]]
+    le2 = [twin.train_step(xt, tt, lr=lr) for lr in lrs[1:]]
+    assert graph.status() == 0 and twin.status() == 0
+    assert graph.step_count == twin.step_count == len(lrs)
+    print("UNET_GRAPH losses graph", [l0] + lg, "eager", [l0] + le2)
+    graph2 = twin
+    for a, b in zip(lg, le2):
+        assert abs(a - b) <= 1e-4 * abs(b), (a, b)
+    for L in net.LAYERS:
+        wa = graph.w[L.name].cpu().numpy()
+        wb = graph2.w[L.name].cpu().numpy()
+        assert rel_l2(wa, wb) <= 1e-4, (L.name, rel_l2(wa, wb))
+    graph.free_graph()
 
 
 HALO_CASES = [(2, 8, 24, 20, 16, 16, 0), (1, 6, 32, 16, 32, 48, 0), (1, 5, 16, 8, 48, 16, 1),
