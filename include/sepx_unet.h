@@ -28,12 +28,25 @@ extern "C" {
 int sepx_unet_packed_elems(int cout, int cin_p, int ntap, int transpose);
 int sepx_unet_pack_weights(const float *w, int cout, int cin_p, int ntap, int transpose, void *out,
                            void *stream);
+/* njobs (<= 64) packings in one launch; the arrays are host arrays of
+ * length njobs, job i as sepx_unet_pack_weights(w[i], cout[i], cin_p[i],
+ * ntap[i], transpose[i], out[i]) */
+int sepx_unet_pack_weights_many(int njobs, const float *const *w, void *const *out, const int *cout,
+                                const int *cin_p, const int *ntap, const int *transpose, void *stream);
 /* y = act(conv(x, w) + bias), ntap 27 (3x3x3, zero padding 1) or 1 (1x1x1),
  * cin = channels read from x (a multiple of 8); y (BF16 view) and/or yf
  * (FP32 [voxels][cout], plus resid[voxels][cout] when resid is not NULL) */
 int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
                        int ntap, const void *wpacked, const float *bias, int cout, int relu, void *y,
                        int y_cstride, int y_coff, float *yf, const float *resid, void *stream);
+/* The same with the ReLU backward fused into the epilogue (for the data
+ * gradient): outputs become 0 where the BF16 view mask (cout channels at
+ * mask_coff) is not > 0 -- bit-identical to sepx_unet_relu_mask afterwards.
+ * mask NULL: no mask.  cout must be a multiple of 8 when mask is given. */
+int sepx_unet_conv_fwd_masked(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
+                              int cin, int ntap, const void *wpacked, const float *bias, int cout, int relu,
+                              void *y, int y_cstride, int y_coff, float *yf, const float *resid,
+                              const void *mask, int mask_cstride, int mask_coff, void *stream);
 /* 3x3x3 layers whose planes are at least 16 x 8 voxels and whose packed
  * weights and input halo fit in 227 KB of shared memory run on the
  * halo-staged kernel, and the weight gradients of 3x3x3 layers with at most
@@ -41,6 +54,12 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
  * enable = 0 sends every layer to the per-tap gather kernels.  Returns the
  * previous setting. */
 int sepx_unet_set_halo(int enable);
+/* Weight-gradient kernel choice (with the halo-staged kernels enabled):
+ * 2 (default) the z-walk tap-stacked kernel (cin <= 48, cout <= 40), else
+ * the per-tile tap-stacked kernel (cin <= 80, cout <= 40), else the gather
+ * kernel; 1 the per-tile kernel, else gather; 0 gather.  Returns the
+ * previous choice, or -1 for another value. */
+int sepx_unet_set_wgrad_form(int form);
 /* dw[t*cin + c][cout] += sum_v x[v + off(t)][c] dy[v][cout]  (FP32
  * accumulation); dy holds cout rounded up to 8 channels at dy_coff */
 int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
@@ -49,8 +68,9 @@ int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D
 /* The same, plus db[cout] += sum_v dy[v][cout] when db is not NULL (taken
  * from the same tiles on the tap-stacked kernel).  The tap-stacked kernel
  * sums per-CTA partials in a fixed order (repeatable results); it keeps them
- * in a library scratch buffer, so calls on different streams must not
- * overlap, and the first call of a shape must not be inside a graph capture. */
+ * in a library scratch buffer (one for the gradient sums, one for the split-K
+ * convolutions), so weight gradients on two streams must not overlap, and the
+ * first call of a shape must not be inside a graph capture. */
 int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
                               int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
                               float *dw, float *db, void *stream);
@@ -59,11 +79,19 @@ int sepx_unet_avgpool(const void *x, int x_cstride, int x_coff, int nb, int D, i
                       void *y, int y_cstride, int y_coff, void *stream);
 int sepx_unet_avgpool_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
                           int c, void *dx, int dx_cstride, int dx_coff, int accumulate, void *stream);
+/* ... then dx = 0 where the BF16 view mask is not > 0 (the ReLU backward of
+ * the layer that produced dx's activation, applied after the sum) */
+int sepx_unet_avgpool_bwd_masked(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
+                                 int c, void *dx, int dx_cstride, int dx_coff, int accumulate,
+                                 const void *mask, int mask_cstride, int mask_coff, void *stream);
 /* nearest x2 upsampling of a (D, H, W) volume and its gradient */
 int sepx_unet_upsample(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int c,
                        void *y, int y_cstride, int y_coff, void *stream);
 int sepx_unet_upsample_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
                            int c, void *dx, int dx_cstride, int dx_coff, void *stream);
+int sepx_unet_upsample_bwd_masked(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
+                                  int c, void *dx, int dx_cstride, int dx_coff, const void *mask,
+                                  int mask_cstride, int mask_coff, void *stream);
 /* dy = 0 where y <= 0 (ReLU backward, in place) */
 int sepx_unet_relu_mask(const void *y, int y_cstride, int y_coff, void *dy, int dy_cstride,
                         int dy_coff, long long V, int c, void *stream);

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "sepx_common.h"
@@ -38,6 +39,17 @@ struct View {
   const __nv_bfloat16 *p;
   int cstride, coff;
 };
+
+// ReLU backward fused into a data-gradient epilogue: the 8 outputs at acc
+// become 0 where the activation (BF16, 8 channels at m) is not > 0 -- the
+// same test as relu_mask_kernel, so the result is bit-identical
+__device__ __forceinline__ void mask8(const __nv_bfloat16 *m, float *acc) {
+  const uint4 q = *reinterpret_cast<const uint4 *>(m);
+  const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+    if (!(__bfloat162float(h[i]) > 0.f)) acc[i] = 0.f;
+}
 
 // Voxel coordinates and the neighbour loads of the implicit GEMMs.  Volumes
 // hold fewer than 2^31 voxels (checked on the host), so voxel indices are
@@ -101,7 +113,8 @@ constexpr int kCS = 3;   // pipeline stages of the convolution kernels
 __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
     View x, int nb, int D, int H, int W, int cin, int ntap, const __nv_bfloat16 *__restrict__ wp,
     int kchunks, const float *__restrict__ bias, int cout, int np, int relu, __nv_bfloat16 *y,
-    int y_cstride, int y_coff, float *yf, const float *resid, int *err) {
+    int y_cstride, int y_coff, float *yf, const float *resid, int *err, int kper, float *kpart,
+    View mask) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -114,6 +127,11 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
   const long long V = (long long)nb * D * H * W;
   const long long v0 = (long long)blockIdx.x * kTM;
   const uint32_t ncols = np <= 32 ? 32 : (np <= 64 ? 64 : 128);
+  // split K (kpart != NULL): this CTA sums K chunks kb .. kb + nk - 1 and
+  // leaves its raw sums in kpart[blockIdx.y][v][np] for conv_finish_kernel
+  const int kb = kpart ? (int)blockIdx.y * kper : 0;
+  const int nk = kpart ? min(kper, kchunks - kb) : kchunks;
+  if (nk <= 0) return;   // uniform for the CTA, before any allocation
 
   if (warp == 0) {
     tc::tmem_alloc(smem_u32(tslot), ncols);
@@ -137,7 +155,8 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
   const Coord cv = coord_of(vr, D, H, W);
   const __nv_bfloat16 *xrow = x.p + (long long)vr * x.cstride + x.coff;
   const int Wc = W * x.cstride, HWc = H * Wc;
-  int tap = 0, c0 = 0;   // K position of the next K group to fetch: tap and channel
+  // K position of the next K group to fetch: tap and channel
+  int tap = (kb * kKC) / cin, c0 = (kb * kKC) % cin;
 
   // chunk j -> stage j % kCS: the A row of this thread (8 K groups of 8
   // channels of one tap, zeros outside the volume) and a share of the
@@ -166,16 +185,16 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
         tap++;
       }
     }
-    const uint4 *wsrc = reinterpret_cast<const uint4 *>(wp + (size_t)j * np * kKC);
+    const uint4 *wsrc = reinterpret_cast<const uint4 *>(wp + (size_t)(kb + j) * np * kKC);
     for (int i = tid; i < b_bytes / 16; i += kUThreads) cp_async16(Bm + 16 * i, wsrc + i, 16);
     cp_async_commit();
   };
 
   for (int j = 0; j < kCS - 1; j++) {
-    if (j < kchunks) fetch(j);
+    if (j < nk) fetch(j);
     else cp_async_commit();
   }
-  for (int j = 0; j < kchunks; j++) {
+  for (int j = 0; j < nk; j++) {
     cp_async_wait<kCS - 2>();   // this thread's copies of chunk j have landed
     tc::fence_proxy_async();
     if (!__syncthreads_and(ok)) break;
@@ -194,7 +213,7 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
     last = j;
     // refill: chunk j + kCS - 1 reuses the stage of chunk j - 1
     const int jn = j + kCS - 1;
-    if (jn < kchunks) {
+    if (jn < nk) {
       if (j >= 1 && !mbar_wait_bounded(smem_u32(&bar[(j - 1) % kCS]), ((j - 1) / kCS) & 1, err,
                                        kErrMmaWait))
         ok = false;
@@ -210,7 +229,7 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
   if (last >= 0) {
     if (!mbar_wait_bounded(smem_u32(&bar[last % kCS]), (last / kCS) & 1, err, kErrMmaWait)) ok = false;
   }
-  if (last != kchunks - 1) ok = false;
+  if (last != nk - 1) ok = false;
   ok = __syncthreads_and(ok);
   tc::fence_after_sync();
   if (ok) {
@@ -219,6 +238,14 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
     for (int n0 = 0; n0 < np; n0 += 16) {
       float acc[16];
       tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + n0, acc);
+      if (kpart) {
+        if (v < V) {
+          float4 *dst = reinterpret_cast<float4 *>(kpart + ((size_t)blockIdx.y * V + v) * np + n0);
+#pragma unroll
+          for (int i = 0; i < 4; i++) dst[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+        }
+        continue;
+      }
       if (v < V) {
 #pragma unroll
         for (int i = 0; i < 16; i++) {
@@ -226,6 +253,11 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
           float o = acc[i] + ((n < cout && bias) ? bias[n] : 0.f);
           if (relu) o = fmaxf(o, 0.f);
           acc[i] = o;
+        }
+        if (mask.p) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 8)
+            if (n0 + i + 8 <= cout) mask8(mask.p + v * mask.cstride + mask.coff + n0 + i, acc + i);
         }
         if (y) {
 #pragma unroll
@@ -251,6 +283,46 @@ __global__ void __launch_bounds__(kUThreads) conv_fwd_kernel(
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// Split-K epilogue: y = act(sum over the splits, in order, + bias); thread:
+// one voxel and 8 output channels
+__global__ void conv_finish_kernel(const float *__restrict__ kpart, int splits, long long V, int np,
+                                   const float *__restrict__ bias, int cout, int relu, __nv_bfloat16 *y,
+                                   int y_cstride, int y_coff, float *yf, const float *resid, View mask) {
+  const int ng = (cout + 7) / 8;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < V * ng;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long v = e / ng;
+    const int n0 = (int)(e % ng) * 8;
+    float acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc[i] = 0.f;
+    for (int k = 0; k < splits; k++) {
+      const float4 *src = reinterpret_cast<const float4 *>(kpart + ((size_t)k * V + v) * np + n0);
+      const float4 a = src[0], b = src[1];
+      acc[0] += a.x; acc[1] += a.y; acc[2] += a.z; acc[3] += a.w;
+      acc[4] += b.x; acc[5] += b.y; acc[6] += b.z; acc[7] += b.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int n = n0 + i;
+      float o = acc[i] + ((n < cout && bias) ? bias[n] : 0.f);
+      acc[i] = relu ? fmaxf(o, 0.f) : o;
+    }
+    if (mask.p && n0 + 8 <= cout) mask8(mask.p + v * mask.cstride + mask.coff + n0, acc);
+    if (y && n0 + 8 <= cout) {
+      __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) h[i] = __float2bfloat16_rn(acc[i]);
+      *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff + n0) = *reinterpret_cast<const uint4 *>(h);
+    }
+    if (yf) {
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if (n0 + i < cout) yf[v * cout + n0 + i] = acc[i] + (resid ? resid[v * cout + n0 + i] : 0.f);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -286,6 +358,7 @@ struct HaloArgs {
   long long ntiles;
   uint32_t wbytes;     // packed weights of all taps
   int nbuf;            // halo buffers: 2 (prefetch during the MMAs) or 1
+  View mask;           // ReLU-backward mask (mask.p NULL: none)
 };
 
 // channel groups held per halo buffer: cin/8 rounded up to even (an odd
@@ -526,6 +599,12 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
             if (a.relu) o = fmaxf(o, 0.f);
             acc[i] = o;
           }
+          if (a.mask.p) {
+#pragma unroll
+            for (int i = 0; i < 16; i += 8)
+              if (n0 + i + 8 <= a.cout)
+                mask8(a.mask.p + v * a.mask.cstride + a.mask.coff + n0 + i, acc + i);
+          }
           if (a.y) {
 #pragma unroll
             for (int i = 0; i < 16; i += 8) {
@@ -714,31 +793,164 @@ __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
 // taps flipped) B[n = c][k = t*cout_p + o] = w[ntap-1-t][c][o], cout_p = cout
 // rounded up to 8.  Packed layout [kchunks][8][np/8][8 n][8 k], zero outside.
 // ---------------------------------------------------------------------------
-__global__ void pack_weights_kernel(const float *__restrict__ w, int cout, int cin_p, int ntap,
-                                    int transpose, int np, int kchunks, __nv_bfloat16 *out) {
-  const int nout = transpose ? cin_p : cout;                   // GEMM N
-  const int kin = transpose ? ((cout + 7) / 8) * 8 : cin_p;    // channels along K
-  const long long total = (long long)kchunks * kKC * np;
+struct PackJob {
+  const float *w;
+  __nv_bfloat16 *out;
+  int cout, cin_p, ntap, transpose, np, kchunks;
+};
+
+__device__ __forceinline__ void pack_one(const PackJob &J, long long e) {
+  const int nout = J.transpose ? J.cin_p : J.cout;                   // GEMM N
+  const int kin = J.transpose ? ((J.cout + 7) / 8) * 8 : J.cin_p;    // channels along K
+  const int kk = (int)(e & 7);
+  const int r = (int)((e >> 3) & 7);
+  const long long rest = e >> 6;
+  const int ng = (int)(rest % (J.np / 8));
+  const long long rest2 = rest / (J.np / 8);
+  const int kg = (int)(rest2 % 8);
+  const int j = (int)(rest2 / 8);
+  const int n = ng * 8 + r;
+  const int k = j * kKC + kg * 8 + kk;
+  const int t = k / kin, c = k - t * kin;
+  float val = 0.f;
+  if (n < nout && t < J.ntap) {
+    if (!J.transpose)
+      val = J.w[((size_t)t * J.cin_p + c) * J.cout + n];
+    else if (c < J.cout)
+      val = J.w[((size_t)(J.ntap - 1 - t) * J.cin_p + n) * J.cout + c];
+  }
+  J.out[e] = __float2bfloat16_rn(val);
+}
+
+__global__ void pack_weights_kernel(const PackJob J) {
+  const long long total = (long long)J.kchunks * kKC * J.np;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int kk = (int)(e & 7);
-    const int r = (int)((e >> 3) & 7);
-    const long long rest = e >> 6;
-    const int ng = (int)(rest % (np / 8));
-    const long long rest2 = rest / (np / 8);
-    const int kg = (int)(rest2 % 8);
-    const int j = (int)(rest2 / 8);
-    const int n = ng * 8 + r;
-    const int k = j * kKC + kg * 8 + kk;
-    const int t = k / kin, c = k - t * kin;
-    float val = 0.f;
-    if (n < nout && t < ntap) {
-      if (!transpose)
-        val = w[((size_t)t * cin_p + c) * cout + n];
-      else if (c < cout)
-        val = w[((size_t)(ntap - 1 - t) * cin_p + n) * cout + c];
+       e += (long long)gridDim.x * blockDim.x)
+    pack_one(J, e);
+}
+
+// up to kMaxPackJobs packings in one launch: blockIdx.y picks the job
+constexpr int kMaxPackJobs = 64;
+struct PackJobs {
+  PackJob j[kMaxPackJobs];
+};
+__global__ void pack_weights_many_kernel(const __grid_constant__ PackJobs P) {
+  const PackJob &J = P.j[blockIdx.y];
+  const long long total = (long long)J.kchunks * kKC * J.np;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x)
+    pack_one(J, e);
+}
+
+// ---------------------------------------------------------------------------
+// 1x1x1 layers with few channels (the output layer 16 -> 1 and its data
+// gradient 8 -> 16): memory-bound, one thread per voxel, weights read once
+// per block from the packed BF16 operand into shared memory, FP32 sums in
+// ascending channel order.  The weight gradient of such a layer: per-thread
+// products summed over the block, per-block partials summed in a fixed order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long packed_index(int n, int k, int np) {
+  return ((((long long)(k / kKC) * 8 + (k % kKC) / 8) * (np / 8) + n / 8) * 8 + n % 8) * 8 + k % 8;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256, 3) conv1x1_kernel(View x, long long V, const __nv_bfloat16 *wp, int np,
+                                                      const float *bias, int relu, __nv_bfloat16 *y,
+                                                      int y_cstride, int y_coff, float *yf,
+                                                      const float *resid, View mask) {
+  __shared__ float w[COUT][CIN];
+  __shared__ float bs[COUT];
+  for (int i = threadIdx.x; i < COUT * CIN; i += blockDim.x) {
+    const int n = i / CIN, k = i % CIN;
+    w[n][k] = __bfloat162float(wp[packed_index(n, k, np)]);
+  }
+  for (int i = threadIdx.x; i < COUT; i += blockDim.x) bs[i] = bias ? bias[i] : 0.f;
+  __syncthreads();
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V;
+       v += (long long)gridDim.x * blockDim.x) {
+    float xin[CIN];
+#pragma unroll
+    for (int g = 0; g < CIN / 8; g++) {
+      const uint4 q = *reinterpret_cast<const uint4 *>(x.p + v * x.cstride + x.coff + 8 * g);
+      const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+      for (int i = 0; i < 8; i++) xin[8 * g + i] = __bfloat162float(h[i]);
     }
-    out[e] = __float2bfloat16_rn(val);
+    float acc[COUT];
+    // weights re-read from shared memory per voxel (broadcast loads), not
+    // held in registers: a memory-bound kernel needs its warps more
+    const volatile float(*wv)[CIN] = w;
+#pragma unroll
+    for (int n = 0; n < COUT; n++) {
+      float t = 0.f;
+#pragma unroll
+      for (int k = 0; k < CIN; k++) t = __fmaf_rn(wv[n][k], xin[k], t);
+      t += bs[n];
+      acc[n] = relu ? fmaxf(t, 0.f) : t;
+    }
+    if (mask.p) {
+#pragma unroll
+      for (int g = 0; g < COUT / 8; g++) mask8(mask.p + v * mask.cstride + mask.coff + 8 * g, acc + 8 * g);
+    }
+    if (y) {
+#pragma unroll
+      for (int g = 0; g < COUT / 8; g++) {
+        __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) h[i] = __float2bfloat16_rn(acc[8 * g + i]);
+        *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff + 8 * g) = *reinterpret_cast<const uint4 *>(h);
+      }
+    }
+    if (yf) {
+#pragma unroll
+      for (int n = 0; n < COUT; n++) yf[v * COUT + n] = acc[n] + (resid ? resid[v * COUT + n] : 0.f);
+    }
+  }
+}
+
+// part[block][(c, n)] = sum over the block's voxels of x[v][c] dy[v][n], and
+// bpart[block][n] = sum of dy[v][n] (the bias gradient)
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) wgrad1x1_kernel(View x, View dy, long long V, float *part,
+                                                       float *bpart) {
+  constexpr int NP = CIN * COUT + COUT;
+  __shared__ float red[8][NP];
+  float acc[NP];
+#pragma unroll
+  for (int i = 0; i < NP; i++) acc[i] = 0.f;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V;
+       v += (long long)gridDim.x * blockDim.x) {
+    float xin[CIN], g[COUT];
+#pragma unroll
+    for (int q8 = 0; q8 < CIN / 8; q8++) {
+      const uint4 q = *reinterpret_cast<const uint4 *>(x.p + v * x.cstride + x.coff + 8 * q8);
+      const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+      for (int i = 0; i < 8; i++) xin[8 * q8 + i] = __bfloat162float(h[i]);
+    }
+#pragma unroll
+    for (int n = 0; n < COUT; n++) g[n] = __bfloat162float(dy.p[v * dy.cstride + dy.coff + n]);
+#pragma unroll
+    for (int c = 0; c < CIN; c++)
+#pragma unroll
+      for (int n = 0; n < COUT; n++) acc[c * COUT + n] = __fmaf_rn(xin[c], g[n], acc[c * COUT + n]);
+#pragma unroll
+    for (int n = 0; n < COUT; n++) acc[CIN * COUT + n] += g[n];
+  }
+  // warp sums (fixed tree), then the 8 warps in order
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NP; i++) {
+    float t = acc[i];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[wid][i] = t;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NP; i += blockDim.x) {
+    float t = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += red[k][i];
+    if (i < CIN * COUT) part[(size_t)blockIdx.x * (CIN * COUT) + i] = t;
+    else bpart[(size_t)blockIdx.x * COUT + (i - CIN * COUT)] = t;
   }
 }
 
@@ -774,7 +986,7 @@ __global__ void avgpool_kernel(View x, int nb, int D, int H, int W, int c, __nv_
 
 // gradient of avgpool: dx (D, H, W) = dy(parent) / 8
 __global__ void avgpool_bwd_kernel(View dy, int nb, int D, int H, int W, int c, __nv_bfloat16 *dx,
-                                   int dx_cstride, int dx_coff, int accumulate) {
+                                   int dx_cstride, int dx_coff, int accumulate, View mask) {
   const int D2 = D / 2, H2 = H / 2, W2 = W / 2, cg = c / 8;
   const long long total = (long long)nb * D * H * W * cg;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
@@ -793,6 +1005,13 @@ __global__ void avgpool_bwd_kernel(View dy, int nb, int D, int H, int W, int c, 
 #pragma unroll
     for (int i = 0; i < 8; i++)
       o[i] = __float2bfloat16_rn(__bfloat162float(h[i]) * 0.125f + (accumulate ? __bfloat162float(ho[i]) : 0.f));
+    if (mask.p) {   // ReLU backward of the layer whose output this is (after the sum)
+      const uint4 qm = *reinterpret_cast<const uint4 *>(mask.p + v * mask.cstride + mask.coff + g * 8);
+      const __nv_bfloat16 *hm = reinterpret_cast<const __nv_bfloat16 *>(&qm);
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if (!(__bfloat162float(hm[i]) > 0.f)) o[i] = __float2bfloat16_rn(0.f);
+    }
     *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(o);
   }
 }
@@ -817,7 +1036,7 @@ __global__ void upsample_kernel(View x, int nb, int D, int H, int W, int c, __nv
 
 // gradient of upsampling: dx (D, H, W) = sum of the 8 children
 __global__ void upsample_bwd_kernel(View dy, int nb, int D, int H, int W, int c, __nv_bfloat16 *dx,
-                                    int dx_cstride, int dx_coff) {
+                                    int dx_cstride, int dx_coff, View mask) {
   const int cg = c / 8;
   const long long total = (long long)nb * D * H * W * cg;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
@@ -838,6 +1057,13 @@ __global__ void upsample_bwd_kernel(View dy, int nb, int D, int H, int W, int c,
     __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) o[i] = __float2bfloat16_rn(acc[i]);
+    if (mask.p) {
+      const uint4 qm = *reinterpret_cast<const uint4 *>(mask.p + v * mask.cstride + mask.coff + g * 8);
+      const __nv_bfloat16 *hm = reinterpret_cast<const __nv_bfloat16 *>(&qm);
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if (!(__bfloat162float(hm[i]) > 0.f)) o[i] = __float2bfloat16_rn(0.f);
+    }
     *reinterpret_cast<uint4 *>(dx + v * dx_cstride + dx_coff + g * 8) = *reinterpret_cast<const uint4 *>(o);
   }
 }
@@ -893,12 +1119,14 @@ __global__ void __launch_bounds__(kBiasThreads) bias_grad_kernel(View dy, long l
   }
 }
 
+// one warp per channel: lane l adds blocks l, l+32, ..; then a fixed shuffle tree
 __global__ void bias_sum_kernel(const float *__restrict__ part, int blocks, int c, float *db) {
-  for (int ch = threadIdx.x; ch < c; ch += blockDim.x) {
-    float t = 0.f;
-    for (int b = 0; b < blocks; b++) t += part[(size_t)b * c + ch];
-    db[ch] += t;
-  }
+  const int ch = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (ch >= c) return;
+  float t = 0.f;
+  for (int b = lane; b < blocks; b += 32) t += part[(size_t)b * c + ch];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) db[ch] += t;
 }
 
 // FP32 volume (one channel) -> BF16 channel-last view channel 0, other
@@ -930,7 +1158,14 @@ __global__ void mse_kernel(const float *out, const float *target, long long V, _
     *reinterpret_cast<uint4 *>(g + v * g_cstride) = *reinterpret_cast<const uint4 *>(o);
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc / (double)V);
+  __shared__ double part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+    atomicAdd(loss, t / (double)V);   // one atomic per block
+  }
 }
 
 // hp (optional): {lr, b1, b2, eps, step} read when the kernel runs, so that a
@@ -1004,6 +1239,7 @@ int np_of(int cout) { return ((cout + 15) / 16) * 16; }
 // shared memory a CTA may have (one CTA per SM for the largest of them).
 constexpr size_t kHaloMaxSmem = 227 * 1024;
 bool g_halo_enabled = true;
+int g_wgrad_form = 2;   // 2: z-walk, else per-tile TMA, else gather; 1: per-tile TMA, else gather; 0: gather
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
 size_t g_smem_per_sm = 0, g_smem_reserved = 0;
@@ -1032,13 +1268,13 @@ int unet_dev_init() {
 // channel-last BF16 view as a 5-D tensor (channels, W, H, D, volumes) with a
 // box of 8 channels x bx x by x bz x 1
 int encode_view(CUtensorMap *tm, const void *p, int cstride, int coff, int chans, int nb, int D, int H,
-                int W, int bx, int by, int bz, const char *what) {
+                int W, int bx, int by, int bz, const char *what, int bc = 8) {
   const __nv_bfloat16 *base = (const __nv_bfloat16 *)p + coff;
   if (reinterpret_cast<uintptr_t>(base) % 16) return set_error("unet %s: view not 16-byte aligned", what);
   const cuuint64_t cs = (cuuint64_t)cstride * 2;
   cuuint64_t dims[5] = {(cuuint64_t)chans, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)nb};
   cuuint64_t strides[4] = {cs, cs * W, cs * W * H, cs * W * H * D};
-  cuuint32_t box[5] = {8, (cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz, 1};
+  cuuint32_t box[5] = {(cuuint32_t)bc, (cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz, 1};
   cuuint32_t es[5] = {1, 1, 1, 1, 1};
   CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(base), dims,
                         strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -1048,30 +1284,34 @@ int encode_view(CUtensorMap *tm, const void *p, int cstride, int coff, int chans
 }
 
 // Device scratch for partial sums, grown on demand (a call inside a CUDA-graph
-// capture must not grow it: run the sequence once before capturing).
-float *g_scratch = nullptr;
-size_t g_scratch_floats = 0;
-int unet_scratch(size_t floats, float **p) {
-  if (floats > g_scratch_floats) {
+// capture must not grow it: run the sequence once before capturing).  Two
+// pools: kScrConv for the split-K convolutions, kScrGrad for the weight and
+// bias gradients -- so that the two kinds may run on different streams
+// (the training step runs its weight gradients beside the data gradients).
+enum { kScrConv = 0, kScrGrad = 1 };
+float *g_scratch[2] = {nullptr, nullptr};
+size_t g_scratch_floats[2] = {0, 0};
+int unet_scratch(int pool, size_t floats, float **p) {
+  if (floats > g_scratch_floats[pool]) {
     float *q = nullptr;
     if (cudaMalloc((void **)&q, floats * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
       return set_error("unet: cannot allocate %zu floats of scratch", floats);
     }
-    if (g_scratch) {
+    if (g_scratch[pool]) {
       cudaDeviceSynchronize();   // nothing may still read the old buffer
-      cudaFree(g_scratch);
+      cudaFree(g_scratch[pool]);
     }
-    g_scratch = q;
-    g_scratch_floats = floats;
+    g_scratch[pool] = q;
+    g_scratch_floats[pool] = floats;
   }
-  *p = g_scratch;
+  *p = g_scratch[pool];
   return 0;
 }
 
 int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
               const void *wpacked, uint32_t wbytes, const float *bias, int cout, int np, int relu,
-              void *y, int y_cstride, int y_coff, float *yf, const float *resid, int *err,
+              void *y, int y_cstride, int y_coff, float *yf, const float *resid, View mask, int *err,
               cudaStream_t st) {
   if (unet_dev_init()) return -1;
   CUtensorMap tm;
@@ -1079,7 +1319,7 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
   HaloArgs a;
   a.nb = nb; a.D = D; a.H = H; a.W = W; a.cin = cin; a.cout = cout; a.np = np; a.relu = relu;
   a.bias = bias; a.y = (__nv_bfloat16 *)y; a.y_cstride = y_cstride; a.y_coff = y_coff;
-  a.yf = yf; a.resid = resid; a.err = err;
+  a.yf = yf; a.resid = resid; a.err = err; a.mask = mask;
   a.ty = (H + kTileY - 1) / kTileY;
   a.tx = (W + kTileX - 1) / kTileX;
   a.ntiles = (long long)nb * D * a.ty * a.tx;
@@ -1122,6 +1362,89 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
   return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
 }
 
+// The z-walk form of the tap-stacked weight gradient (sepx_unet_wgrad.inc)
+// for cin <= 48 and 8 ngo <= 40.  Returns 1 where it does not apply.
+int conv_wgrad_zw(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
+                  const void *dy, int dy_cstride, int dy_coff, int cout, float *dw, float *db, int *err,
+                  cudaStream_t st) {
+  const int ngi = cin / 8, ngo = (cout + 7) / 8;
+  if (!g_halo_enabled || g_wgrad_form < 2 || 3 * ngo > 16 || ngi > 6) return 1;
+  if (unet_dev_init()) return -1;
+  ZwArgs a;
+  a.nb = nb; a.D = D; a.H = H; a.W = W; a.cin = cin; a.cout = cout; a.ngi = ngi; a.ngo = ngo;
+  a.np = ((8 * (3 * ngi + 1)) + 15) / 16 * 16;
+  if (3 * a.np > 512) return 1;
+  a.a_bytes = 3u * ngo * kWgBox;
+  a.pl_bytes = (uint32_t)(a.np / 8) * kWgBox;
+  a.rawb_bytes = 18u * 8u * (uint32_t)cin * 2u;
+  a.rawa_bytes = 16u * 10u * 8u * (uint32_t)ngo * 2u;
+  a.raw_bytes = (a.rawb_bytes + a.rawa_bytes + 127u) / 128u * 128u;
+  const size_t fixed = 2 * (size_t)a.a_bytes + 4 * (size_t)a.pl_bytes + (2 * kZwMaxRaw + 12) * 8 + 16 + 128;
+  if (fixed + 2 * (size_t)a.raw_bytes > kHaloMaxSmem) return 1;
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(3 * a.np)) ncols <<= 1;
+  // raw slots: as many as keep the most CTAs per SM (by shared and tensor memory)
+  auto per_sm_of = [&](int nr) {
+    const size_t sm = fixed + (size_t)nr * a.raw_bytes;
+    if (sm > kHaloMaxSmem) return 0;
+    const int k = (int)(g_smem_per_sm / (((sm + 127) / 128) * 128 + g_smem_reserved));
+    return std::min(k, 512 / (int)ncols);
+  };
+  a.nraw = 2;
+  for (int nr = 3; nr <= kZwMaxRaw; nr++)
+    if (per_sm_of(nr) >= per_sm_of(a.nraw)) a.nraw = nr;
+  const size_t smem = fixed + (size_t)a.nraw * a.raw_bytes;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(conv_wgrad_zw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kHaloMaxSmem);
+    if (e != cudaSuccess) return set_error("unet wgrad: %s", cudaGetErrorString(e));
+    attr = true;
+  }
+  const int per_sm = per_sm_of(a.nraw);
+  if (per_sm < 1) return 1;
+  const long long slots = (long long)g_num_sms * per_sm;
+  a.ty = (H + 15) / 16;
+  a.tx = (W + 2 + 7) / 8;
+  // planes per window: few windows leave SMs idle, short ones reload more
+  // planes (zc + 2 per zc tiles); take the z run with the least work on the
+  // busiest CTA, counting a plane as a third of a tile
+  const long long cols = (long long)nb * a.ty * a.tx;
+  double best = 1e300;
+  for (int zc = D;; zc = (zc + 1) / 2) {
+    const long long nzc = (D + zc - 1) / zc;
+    const long long items = cols * nzc;
+    const long long per = (items + slots - 1) / slots;
+    const double cost = (double)per * (zc + 2.0 / 3.0);
+    if (cost < best) {
+      best = cost;
+      a.zc = zc;
+      a.nzc = (int)nzc;
+    }
+    if (zc <= 4) break;
+  }
+  a.nitems = cols * a.nzc;
+  const long long grid = a.nitems < slots ? a.nitems : slots;
+  a.err = err;
+  a.mrows = 3 * 8 * ngo <= 64 ? 64 : 128;
+  CUtensorMap tmx, tmy;
+  if (encode_view(&tmx, x, x_cstride, x_coff, cin, nb, D, H, W, 8, 18, 1, "wgrad x", cin) ||
+      encode_view(&tmy, dy, dy_cstride, dy_coff, 8 * ngo, nb, D, H, W, 10, 16, 1, "wgrad dy", 8 * ngo))
+    return -1;
+  const long long n = 27LL * cin * cout;
+  float *scr;
+  if (unet_scratch(kScrGrad, (size_t)grid * (size_t)(n + cout), &scr)) return -1;
+  a.part = scr;
+  a.bpart = scr + (size_t)grid * n;
+  conv_wgrad_zw_kernel<<<(unsigned)grid, kZwThreads, smem, st>>>(tmx, tmy, a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error("unet wgrad: %s", cudaGetErrorString(e));
+  wg_reduce_kernel<<<(unsigned)((n + cout + 31) / 32), 32 * kRedSlices, 0, st>>>(a.part, (int)grid, n, dw,
+                                                                             a.bpart, cout, db);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet wgrad: %s", cudaGetErrorString(e));
+}
+
 // The tap-stacked TMA weight gradient (sepx_unet_wgrad.inc) for 3x3x3 layers
 // with 3 x (cout rounded to 8) <= 128 rows and 3 x cin / 8 + 1 N groups <= 32.
 // Returns 1 where it does not apply (the caller takes the gather kernel).
@@ -1129,7 +1452,7 @@ int conv_wgrad_tma(const void *x, int x_cstride, int x_coff, int nb, int D, int 
                    const void *dy, int dy_cstride, int dy_coff, int cout, float *dw, float *db, int *err,
                    cudaStream_t st) {
   const int ngi = cin / 8, ngo = (cout + 7) / 8;
-  if (!g_halo_enabled || 3 * ngo > 16 || 3 * ngi + 1 > 32) return 1;
+  if (!g_halo_enabled || g_wgrad_form < 1 || 3 * ngo > 16 || 3 * ngi + 1 > 32) return 1;
   if (unet_dev_init()) return -1;
   const int np = ((8 * (3 * ngi + 1)) + 15) / 16 * 16;
   const uint32_t a_bytes = 3u * ngo * kWgBox;
@@ -1187,17 +1510,17 @@ int conv_wgrad_tma(const void *x, int x_cstride, int x_coff, int nb, int D, int 
   a.b_bytes = (uint32_t)ndz * (np / 8) * kWgBox;
   a.stage_bytes = stage;
   a.err = err;
+  a.mrows = 3 * 8 * ngo <= 64 ? 64 : 128;
   const long long n = 27LL * cin * cout;
   float *scr;
-  if (unet_scratch((size_t)a.groups * (size_t)(n + cout), &scr)) return -1;
+  if (unet_scratch(kScrGrad, (size_t)a.groups * (size_t)(n + cout), &scr)) return -1;
   a.part = scr;
   a.bpart = scr + (size_t)a.groups * n;
   conv_wgrad_tma_kernel<<<(unsigned)(a.groups * nzg), kWgThreads, smem, st>>>(tmx, tmy, a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error("unet wgrad: %s", cudaGetErrorString(e));
   const long long tot = n + cout;
-  wg_reduce_kernel<<<(unsigned)((tot + 255) / 256 < 1216 ? (tot + 255) / 256 : 1216), 256, 0, st>>>(
-      a.part, a.groups, n, dw, a.bpart, cout, db);
+  wg_reduce_kernel<<<(unsigned)((tot + 31) / 32), 32 * kRedSlices, 0, st>>>(a.part, a.groups, n, dw, a.bpart, cout, db);
   e = cudaGetLastError();
   return e == cudaSuccess ? 0 : set_error("unet wgrad: %s", cudaGetErrorString(e));
 }
@@ -1209,10 +1532,10 @@ int bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V, int c, f
   long long blocks = (V + lanes - 1) / lanes;
   if (blocks > 2 * 152) blocks = 2 * 152;
   float *scr;
-  if (unet_scratch((size_t)blocks * c, &scr)) return -1;
+  if (unet_scratch(kScrGrad, (size_t)blocks * c, &scr)) return -1;
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
   bias_grad_kernel<<<(unsigned)blocks, kBiasThreads, 0, st>>>(dv, V, c, scr);
-  bias_sum_kernel<<<1, 128, 0, st>>>(scr, (int)blocks, c, db);
+  bias_sum_kernel<<<(c + 3) / 4, 128, 0, st>>>(scr, (int)blocks, c, db);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet bias_grad: launch failed");
 }
 }  // namespace
@@ -1230,6 +1553,13 @@ int need_dims(int nb, int D, int H, int W, const char *what) {
 }  // namespace
 
 extern "C" {
+
+int sepx_unet_set_wgrad_form(int form) {
+  if (form < 0 || form > 2) return set_error("unet: weight-gradient form %d (0, 1 or 2)", form);
+  const int prev = g_wgrad_form;
+  g_wgrad_form = form;
+  return prev;
+}
 
 int sepx_unet_set_halo(int enable) {
   const int prev = g_halo_enabled ? 1 : 0;
@@ -1250,8 +1580,31 @@ int sepx_unet_pack_weights(const float *w, int cout, int cin_p, int ntap, int tr
   if (cout < 1 || cin_p < 8 || nout > kMaxN || cin_p % 8 || (ntap != 1 && ntap != 27))
     return set_error("unet pack: channels (%d -> %d) unsupported", kin, nout);
   const int np = np_of(nout), kch = (ntap * kin + kKC - 1) / kKC;
-  pack_weights_kernel<<<grid_for((long long)kch * kKC * np), 256, 0, (cudaStream_t)stream>>>(
-      w, cout, cin_p, ntap, transpose, np, kch, (__nv_bfloat16 *)out);
+  PackJob J{w, (__nv_bfloat16 *)out, cout, cin_p, ntap, transpose, np, kch};
+  pack_weights_kernel<<<grid_for((long long)kch * kKC * np), 256, 0, (cudaStream_t)stream>>>(J);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : set_error("unet pack: %s", cudaGetErrorString(e));
+}
+
+int sepx_unet_pack_weights_many(int njobs, const float *const *w, void *const *out, const int *cout,
+                                const int *cin_p, const int *ntap, const int *transpose, void *stream) {
+  if (njobs < 0 || njobs > kMaxPackJobs) return set_error("unet pack: %d jobs (at most %d)", njobs, kMaxPackJobs);
+  if (njobs == 0) return 0;
+  if (!w || !out || !cout || !cin_p || !ntap || !transpose) return set_error("unet pack: NULL job array");
+  PackJobs P;
+  long long most = 0;
+  for (int i = 0; i < njobs; i++) {
+    if (need_dev(w[i], "pack weights w") || need_dev(out[i], "pack weights out")) return -1;
+    const int tr = transpose[i] ? 1 : 0;
+    const int nout = tr ? cin_p[i] : cout[i], kin = tr ? ((cout[i] + 7) / 8) * 8 : cin_p[i];
+    if (cout[i] < 1 || cin_p[i] < 8 || nout > kMaxN || cin_p[i] % 8 || (ntap[i] != 1 && ntap[i] != 27))
+      return set_error("unet pack: job %d: channels (%d -> %d) unsupported", i, kin, nout);
+    const int np = np_of(nout), kch = (ntap[i] * kin + kKC - 1) / kKC;
+    P.j[i] = PackJob{w[i], (__nv_bfloat16 *)out[i], cout[i], cin_p[i], ntap[i], tr, np, kch};
+    most = std::max(most, (long long)kch * kKC * np);
+  }
+  const long long bx = std::min<long long>((most + 255) / 256, 64);
+  pack_weights_many_kernel<<<dim3((unsigned)bx, (unsigned)njobs), 256, 0, (cudaStream_t)stream>>>(P);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : set_error("unet pack: %s", cudaGetErrorString(e));
 }
@@ -1259,8 +1612,19 @@ int sepx_unet_pack_weights(const float *w, int cout, int cin_p, int ntap, int tr
 int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W, int cin,
                        int ntap, const void *wpacked, const float *bias, int cout, int relu, void *y,
                        int y_cstride, int y_coff, float *yf, const float *resid, void *stream) {
+  return sepx_unet_conv_fwd_masked(x, x_cstride, x_coff, nb, D, H, W, cin, ntap, wpacked, bias, cout, relu, y,
+                                   y_cstride, y_coff, yf, resid, nullptr, 0, 0, stream);
+}
+
+int sepx_unet_conv_fwd_masked(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
+                              int cin, int ntap, const void *wpacked, const float *bias, int cout, int relu,
+                              void *y, int y_cstride, int y_coff, float *yf, const float *resid,
+                              const void *mask, int mask_cstride, int mask_coff, void *stream) {
   if (need_dev(x, "conv x") || need_dev(wpacked, "conv weights") || need_dims(nb, D, H, W, "conv"))
     return -1;
+  if (mask && (cout % 8 || mask_cstride % 8 || mask_coff % 8 || mask_coff + cout > mask_cstride))
+    return set_error("unet conv: bad mask view");
+  const View mv{(const __nv_bfloat16 *)mask, mask_cstride, mask_coff};
   if (!y && !yf) return set_error("unet conv: no output (y and yf are NULL)");
   if (check_conv_args(cin, x_cstride, x_coff, cout, ntap))
     return set_error("unet conv: bad channel arguments (cin %d cstride %d coff %d cout %d ntap %d)", cin,
@@ -1282,7 +1646,20 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
     const uint32_t wbytes = (uint32_t)((27 * ngc + (ngc & 1)) * (np / 8) * 128);
     if (halo_smem_bytes(cin, wbytes, 1) <= kHaloMaxSmem)
       return conv_halo(x, x_cstride, x_coff, nb, D, H, W, cin, wpacked, wbytes, bias, cout, np, relu, y,
-                       y_cstride, y_coff, yf, resid, err, (cudaStream_t)stream);
+                       y_cstride, y_coff, yf, resid, mv, err, (cudaStream_t)stream);
+  }
+  if (ntap == 1 && g_halo_enabled && ((cin == 16 && cout == 1 && !y) || (cin == 8 && cout == 16))) {
+    View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
+    const unsigned grid = (unsigned)std::min<long long>((V + 255) / 256, 4 * 152);
+    if (cin == 16)
+      conv1x1_kernel<16, 1><<<grid, 256, 0, (cudaStream_t)stream>>>(
+          xv, V, (const __nv_bfloat16 *)wpacked, np, bias, relu, nullptr, 0, 0, yf, resid, mv);
+    else
+      conv1x1_kernel<8, 16><<<grid, 256, 0, (cudaStream_t)stream>>>(
+          xv, V, (const __nv_bfloat16 *)wpacked, np, bias, relu, (__nv_bfloat16 *)y, y_cstride, y_coff, yf,
+          resid, mv);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
   }
   const size_t smem = conv_smem(np);
   static bool attr = false;
@@ -1293,9 +1670,31 @@ int sepx_unet_conv_fwd(const void *x, int x_cstride, int x_coff, int nb, int D, 
     attr = true;
   }
   View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
-  conv_fwd_kernel<<<(unsigned)((V + kTM - 1) / kTM), kUThreads, smem, (cudaStream_t)stream>>>(
-      xv, nb, D, H, W, cin, ntap, (const __nv_bfloat16 *)wpacked, kch, bias, cout, np, relu,
-      (__nv_bfloat16 *)y, y_cstride, y_coff, yf, resid, err);
+  const long long mt = (V + kTM - 1) / kTM;
+  // few voxel tiles (the coarse levels): split K over CTAs so that about two
+  // CTAs per SM run, at least two K chunks each; the splits' FP32 sums are
+  // added in order by conv_finish_kernel
+  int splits = 1, kper = kch;
+  if (g_halo_enabled && mt < 2 * 152 && kch >= 4) {
+    splits = (int)std::min<long long>((2 * 152 + mt - 1) / mt, kch / 2);
+    kper = (kch + splits - 1) / splits;
+    splits = (kch + kper - 1) / kper;
+  }
+  if (splits > 1) {
+    float *kpart;
+    if (unet_scratch(kScrConv, (size_t)splits * V * np, &kpart)) return -1;
+    conv_fwd_kernel<<<dim3((unsigned)mt, (unsigned)splits), kUThreads, smem, (cudaStream_t)stream>>>(
+        xv, nb, D, H, W, cin, ntap, (const __nv_bfloat16 *)wpacked, kch, bias, cout, np, relu,
+        (__nv_bfloat16 *)y, y_cstride, y_coff, yf, resid, err, kper, kpart, mv);
+    const long long work = V * ((cout + 7) / 8);
+    conv_finish_kernel<<<(unsigned)std::min<long long>((work + 255) / 256, 8 * 152), 256, 0,
+                         (cudaStream_t)stream>>>(kpart, splits, V, np, bias, cout, relu,
+                                                 (__nv_bfloat16 *)y, y_cstride, y_coff, yf, resid, mv);
+  } else {
+    conv_fwd_kernel<<<(unsigned)mt, kUThreads, smem, (cudaStream_t)stream>>>(
+        xv, nb, D, H, W, cin, ntap, (const __nv_bfloat16 *)wpacked, kch, bias, cout, np, relu,
+        (__nv_bfloat16 *)y, y_cstride, y_coff, yf, resid, err, kch, nullptr, mv);
+  }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : set_error("unet conv: %s", cudaGetErrorString(e));
 }
@@ -1323,16 +1722,35 @@ int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, 
   if (V >= (1LL << 31) || (long long)H * W * x_cstride >= (1LL << 30))
     return set_error("unet wgrad: volume too large (%lld voxels)", V);
   if (ntap == 27) {
-    const int rc = conv_wgrad_tma(x, x_cstride, x_coff, nb, D, H, W, cin, dy, dy_cstride, dy_coff, cout,
-                                  dw, db, err, (cudaStream_t)stream);
+    int rc = conv_wgrad_zw(x, x_cstride, x_coff, nb, D, H, W, cin, dy, dy_cstride, dy_coff, cout, dw, db,
+                           err, (cudaStream_t)stream);
     if (rc <= 0) return rc;
+    rc = conv_wgrad_tma(x, x_cstride, x_coff, nb, D, H, W, cin, dy, dy_cstride, dy_coff, cout, dw, db, err,
+                        (cudaStream_t)stream);
+    if (rc <= 0) return rc;
+  }
+  if (ntap == 1 && cin == 16 && cout == 1 && g_halo_enabled) {
+    constexpr int NP = 16 * 1 + 1;
+    const long long blocks = std::min<long long>((V + 255) / 256, 2 * 152);
+    float *scr;
+    if (unet_scratch(kScrGrad, (size_t)blocks * NP, &scr)) return -1;
+    View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
+    View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+    float *bscr = scr + (size_t)blocks * 16;
+    wgrad1x1_kernel<16, 1><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(xv, dv, V, scr, bscr);
+    // the same fixed-order sum as the tap-stacked kernels
+    wg_reduce_kernel<<<1, 32 * kRedSlices, 0, (cudaStream_t)stream>>>(scr, (int)blocks, 16, dw, bscr, 1, db);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : set_error("unet wgrad: %s", cudaGetErrorString(e));
   }
   if (db && bias_grad(dy, dy_cstride, dy_coff, V, cout, db, (cudaStream_t)stream)) return -1;
   const long long vchunks = (V + kKC - 1) / kKC;
   const int mt = (ntap * cin + kTM - 1) / kTM;
-  // enough CTAs to fill the GPU about twice, at least 16 voxel chunks each
+  // enough CTAs to fill the GPU about twice, with at least 16 voxel chunks
+  // each (fewer on the smallest volumes: at least 4, and 8 splits); every
+  // split adds its sums with FP32 atomics, so more splits cost contention
   long long per = (vchunks * mt + 2 * 152 * 4 - 1) / (2 * 152 * 4);
-  if (per < 16) per = 16;
+  per = std::max(per, std::max(4LL, std::min(16LL, vchunks / 8)));
   const long long splits = (vchunks + per - 1) / per;
   const size_t smem = conv_smem(np);
   static bool attr = false;
@@ -1363,13 +1781,23 @@ int sepx_unet_avgpool(const void *x, int x_cstride, int x_coff, int nb, int D, i
 
 int sepx_unet_avgpool_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
                           int c, void *dx, int dx_cstride, int dx_coff, int accumulate, void *stream) {
+  return sepx_unet_avgpool_bwd_masked(dy, dy_cstride, dy_coff, nb, D, H, W, c, dx, dx_cstride, dx_coff,
+                                      accumulate, nullptr, 0, 0, stream);
+}
+
+int sepx_unet_avgpool_bwd_masked(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
+                                 int c, void *dx, int dx_cstride, int dx_coff, int accumulate,
+                                 const void *mask, int mask_cstride, int mask_coff, void *stream) {
   if (need_dev(dy, "avgpool_bwd dy") || need_dev(dx, "avgpool_bwd dx") ||
       need_dims(nb, D, H, W, "avgpool_bwd"))
     return -1;
   if (c % 8 || D % 2 || H % 2 || W % 2) return set_error("unet avgpool_bwd: bad shape");
+  if (mask && (mask_cstride % 8 || mask_coff % 8 || mask_coff + c > mask_cstride))
+    return set_error("unet avgpool_bwd: bad mask view");
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  View mv{(const __nv_bfloat16 *)mask, mask_cstride, mask_coff};
   avgpool_bwd_kernel<<<grid_for((long long)nb * D * H * W * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
-      dv, nb, D, H, W, c, (__nv_bfloat16 *)dx, dx_cstride, dx_coff, accumulate);
+      dv, nb, D, H, W, c, (__nv_bfloat16 *)dx, dx_cstride, dx_coff, accumulate, mv);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet avgpool_bwd: launch failed");
 }
 
@@ -1386,13 +1814,23 @@ int sepx_unet_upsample(const void *x, int x_cstride, int x_coff, int nb, int D, 
 
 int sepx_unet_upsample_bwd(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
                            int c, void *dx, int dx_cstride, int dx_coff, void *stream) {
+  return sepx_unet_upsample_bwd_masked(dy, dy_cstride, dy_coff, nb, D, H, W, c, dx, dx_cstride, dx_coff,
+                                       nullptr, 0, 0, stream);
+}
+
+int sepx_unet_upsample_bwd_masked(const void *dy, int dy_cstride, int dy_coff, int nb, int D, int H, int W,
+                                  int c, void *dx, int dx_cstride, int dx_coff, const void *mask,
+                                  int mask_cstride, int mask_coff, void *stream) {
   if (need_dev(dy, "upsample_bwd dy") || need_dev(dx, "upsample_bwd dx") ||
       need_dims(nb, D, H, W, "upsample_bwd"))
     return -1;
   if (c % 8) return set_error("unet upsample_bwd: bad shape");
+  if (mask && (mask_cstride % 8 || mask_coff % 8 || mask_coff + c > mask_cstride))
+    return set_error("unet upsample_bwd: bad mask view");
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
+  View mv{(const __nv_bfloat16 *)mask, mask_cstride, mask_coff};
   upsample_bwd_kernel<<<grid_for((long long)nb * D * H * W * (c / 8)), 256, 0, (cudaStream_t)stream>>>(
-      dv, nb, D, H, W, c, (__nv_bfloat16 *)dx, dx_cstride, dx_coff);
+      dv, nb, D, H, W, c, (__nv_bfloat16 *)dx, dx_cstride, dx_coff, mv);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet upsample_bwd: launch failed");
 }
 
@@ -1434,8 +1872,8 @@ int sepx_unet_mse(const float *out, const float *target, long long V, void *g, i
   if (need_dev(out, "mse out") || need_dev(target, "mse target") || need_dev(g, "mse g") ||
       need_dev(loss, "mse loss"))
     return -1;
-  mse_kernel<<<grid_for(V), 256, 0, (cudaStream_t)stream>>>(out, target, V, (__nv_bfloat16 *)g,
-                                                            g_cstride, loss);
+  mse_kernel<<<grid_for(V) < 2 * 152 ? grid_for(V) : 2 * 152, 256, 0, (cudaStream_t)stream>>>(
+      out, target, V, (__nv_bfloat16 *)g, g_cstride, loss);
   return cudaGetLastError() == cudaSuccess ? 0 : set_error("unet mse: launch failed");
 }
 

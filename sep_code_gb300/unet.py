@@ -37,14 +37,19 @@ _f = C.c_float
 _SIGS = {
     "sepx_unet_packed_elems": [_i, _i, _i, _i],
     "sepx_unet_pack_weights": [_vp, _i, _i, _i, _i, _vp, _vp],
+    "sepx_unet_pack_weights_many": [_i, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "sepx_unet_conv_fwd": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _i, _i, _vp,
                            _vp, _vp],
+    "sepx_unet_conv_fwd_masked": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _i, _i,
+                                  _vp, _vp, _vp, _i, _i, _vp],
     "sepx_unet_conv_wgrad": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp, _vp],
     "sepx_unet_conv_wgrad_bias": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp, _vp, _vp],
     "sepx_unet_avgpool": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _vp],
     "sepx_unet_avgpool_bwd": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp],
     "sepx_unet_upsample": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _vp],
     "sepx_unet_upsample_bwd": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _vp],
+    "sepx_unet_upsample_bwd_masked": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _vp, _i, _i, _vp],
+    "sepx_unet_avgpool_bwd_masked": [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _i, _i, _vp, _i, _i, _vp],
     "sepx_unet_relu_mask": [_vp, _i, _i, _vp, _i, _i, _ll, _i, _vp],
     "sepx_unet_bias_grad": [_vp, _i, _i, _ll, _i, _vp, _vp],
     "sepx_unet_to_bf16": [_vp, _ll, _f, _vp, _i, _i, _vp],
@@ -57,6 +62,7 @@ _SIGS = {
     "sepx_unet_graph_free": [_vp],
     "sepx_unet_status": [],
     "sepx_unet_set_halo": [_i],
+    "sepx_unet_set_wgrad_form": [_i],
 }
 for _n, _a in _SIGS.items():
     getattr(lib, _n).argtypes = _a
@@ -160,15 +166,30 @@ class UNet3D:
         self.step_count = 0
         self.shape = None
         self.graph, self.graph_io = None, None
+        # the weight gradients run on a second stream beside the data
+        # gradients (each forks from the main stream once its dy is ready; the
+        # main stream joins it at the end of the backward pass)
+        self.stream2 = torch.cuda.Stream(device=self.dev)
+        self.stream2_ptr = C.c_void_p(self.stream2.cuda_stream)
+        self._events = [torch.cuda.Event() for _ in range(len(LAYERS) + 1)]
+        self._nev = 0
         self.pack()
 
     # ---------------------------------------------------------------- params
     def pack(self):
-        for L in LAYERS:
-            _chk(lib.sepx_unet_pack_weights(_p(self.w[L.name]), L.cout, L.cin_p, L.ntap, 0,
-                                            _p(self.pk[L.name]), self.stream_ptr))
-            _chk(lib.sepx_unet_pack_weights(_p(self.w[L.name]), L.cout, L.cin_p, L.ntap, 1,
-                                            _p(self.pkt[L.name]), self.stream_ptr))
+        """BF16 forward and data-gradient operands of every layer, one launch"""
+        if getattr(self, "_pack_jobs", None) is None:
+            n = 2 * len(LAYERS)
+            P, I = C.c_void_p * n, C.c_int * n
+            w, out, co, ci, nt, tr = P(), P(), I(), I(), I(), I()
+            for i, L in enumerate(LAYERS):
+                for k, dst in enumerate((self.pk, self.pkt)):
+                    j = 2 * i + k
+                    w[j], out[j] = self.w[L.name].data_ptr(), dst[L.name].data_ptr()
+                    co[j], ci[j], nt[j], tr[j] = L.cout, L.cin_p, L.ntap, k
+            self._pack_jobs = (n, w, out, co, ci, nt, tr)
+        n, w, out, co, ci, nt, tr = self._pack_jobs
+        _chk(lib.sepx_unet_pack_weights_many(n, w, out, co, ci, nt, tr, self.stream_ptr))
 
     def params(self) -> dict:
         self.stream.synchronize()
@@ -234,20 +255,33 @@ class UNet3D:
                                     _p(yf) if yf is not None else None,
                                     _p(resid) if resid is not None else None, self.stream_ptr))
 
-    def _dgrad(self, L, dy, dycs, dyco, lvl, dx, dxcs, dxco):
-        """dx = conv^T(dy): the forward kernel with the transposed, flipped operand."""
+    def _dgrad(self, L, dy, dycs, dyco, lvl, dx, dxcs, dxco, mask=None):
+        """dx = conv^T(dy): the forward kernel with the transposed, flipped
+        operand; mask = (y, ycs, yco): the ReLU backward of the layer below,
+        fused (dx = 0 where y <= 0)."""
         nb = self.shape[0]
         D, H, W = self.dims[lvl]
-        _chk(lib.sepx_unet_conv_fwd(_p(dy), dycs, dyco, nb, D, H, W, _r8(L.cout), L.ntap,
-                                    _p(self.pkt[L.name]), None, L.cin_p, 0, _p(dx), dxcs, dxco,
-                                    None, None, self.stream_ptr))
+        m, mcs, mco = (None, 0, 0) if mask is None else (_p(mask[0]), mask[1], mask[2])
+        _chk(lib.sepx_unet_conv_fwd_masked(_p(dy), dycs, dyco, nb, D, H, W, _r8(L.cout), L.ntap,
+                                           _p(self.pkt[L.name]), None, L.cin_p, 0, _p(dx), dxcs, dxco,
+                                           None, None, m, mcs, mco, self.stream_ptr))
+
+    def _event(self):
+        e = self._events[self._nev % len(self._events)]
+        self._nev += 1
+        return e
 
     def _wgrad(self, L, x, xcs, xco, dy, dycs, dyco, lvl):
+        """weight and bias gradient on the second stream, after everything the
+        main stream has enqueued so far (dy is ready there)"""
         nb = self.shape[0]
         D, H, W = self.dims[lvl]
+        e = self._event()
+        e.record(self.stream)
+        self.stream2.wait_event(e)
         _chk(lib.sepx_unet_conv_wgrad_bias(_p(x), xcs, xco, nb, D, H, W, L.cin_p, L.ntap, _p(dy), dycs,
                                            dyco, L.cout, _p(self.gw[L.name]), _p(self.gb[L.name]),
-                                           self.stream_ptr))
+                                           self.stream2_ptr))
 
     def _relu_mask(self, y, ycs, yco, dy, dycs, dyco, lvl, c):
         _chk(lib.sepx_unet_relu_mask(_p(y), ycs, yco, _p(dy), dycs, dyco, self.V[lvl], c,
@@ -258,11 +292,12 @@ class UNet3D:
         D, H, W = self.dims[lvl]
         _chk(lib.sepx_unet_avgpool(_p(x), xcs, xco, nb, D, H, W, c, _p(y), ycs, yco, self.stream_ptr))
 
-    def _pool_bwd(self, dy, dycs, dyco, lvl, c, dx, dxcs, dxco, acc):
+    def _pool_bwd(self, dy, dycs, dyco, lvl, c, dx, dxcs, dxco, acc, mask=None):
         nb = self.shape[0]
         D, H, W = self.dims[lvl]
-        _chk(lib.sepx_unet_avgpool_bwd(_p(dy), dycs, dyco, nb, D, H, W, c, _p(dx), dxcs, dxco,
-                                       1 if acc else 0, self.stream_ptr))
+        m, mcs, mco = (None, 0, 0) if mask is None else (_p(mask[0]), mask[1], mask[2])
+        _chk(lib.sepx_unet_avgpool_bwd_masked(_p(dy), dycs, dyco, nb, D, H, W, c, _p(dx), dxcs, dxco,
+                                              1 if acc else 0, m, mcs, mco, self.stream_ptr))
 
     def _up(self, x, xcs, xco, lvl, c, y, ycs, yco):
         """nearest x2 upsampling from level lvl to lvl-1"""
@@ -270,11 +305,12 @@ class UNet3D:
         D, H, W = self.dims[lvl]
         _chk(lib.sepx_unet_upsample(_p(x), xcs, xco, nb, D, H, W, c, _p(y), ycs, yco, self.stream_ptr))
 
-    def _up_bwd(self, dy, dycs, dyco, lvl, c, dx, dxcs, dxco):
+    def _up_bwd(self, dy, dycs, dyco, lvl, c, dx, dxcs, dxco, mask=None):
         nb = self.shape[0]
         D, H, W = self.dims[lvl]
-        _chk(lib.sepx_unet_upsample_bwd(_p(dy), dycs, dyco, nb, D, H, W, c, _p(dx), dxcs, dxco,
-                                        self.stream_ptr))
+        m, mcs, mco = (None, 0, 0) if mask is None else (_p(mask[0]), mask[1], mask[2])
+        _chk(lib.sepx_unet_upsample_bwd_masked(_p(dy), dycs, dyco, nb, D, H, W, c, _p(dx), dxcs, dxco,
+                                               m, mcs, mco, self.stream_ptr))
 
     # ---------------------------------------------------------------- network
     def forward_device(self, xf, scale: float = 1.0):
@@ -321,61 +357,51 @@ class UNet3D:
         a, g, Ly = self.a, self.g, {L.name: L for L in LAYERS}
         # output layer (1x1x1, no ReLU)
         self._wgrad(Ly["out"], a["d1b"], 16, 0, g["out"], 8, 0, 0)
-        self._dgrad(Ly["out"], g["out"], 8, 0, 0, g["d1b"], 16, 0)
+        self._dgrad(Ly["out"], g["out"], 8, 0, 0, g["d1b"], 16, 0, mask=(a["d1b"], 16, 0))
         # level 1 decoder
-        self._relu_mask(a["d1b"], 16, 0, g["d1b"], 16, 0, 0, 16)
         self._wgrad(Ly["d1b"], a["d1a"], 16, 0, g["d1b"], 16, 0, 0)
-        self._dgrad(Ly["d1b"], g["d1b"], 16, 0, 0, g["d1a"], 16, 0)
-        self._relu_mask(a["d1a"], 16, 0, g["d1a"], 16, 0, 0, 16)
+        self._dgrad(Ly["d1b"], g["d1b"], 16, 0, 0, g["d1a"], 16, 0, mask=(a["d1a"], 16, 0))
         self._wgrad(Ly["d1a"], a["cat1"], 48, 0, g["d1a"], 16, 0, 0)
         self._dgrad(Ly["d1a"], g["d1a"], 16, 0, 0, g["cat1"], 48, 0)
-        self._up_bwd(g["cat1"], 48, 0, 1, 32, g["d2b"], 32, 0)
+        self._up_bwd(g["cat1"], 48, 0, 1, 32, g["d2b"], 32, 0, mask=(a["d2b"], 32, 0))
         # level 2 decoder
-        self._relu_mask(a["d2b"], 32, 0, g["d2b"], 32, 0, 1, 32)
         self._wgrad(Ly["d2b"], a["d2a"], 32, 0, g["d2b"], 32, 0, 1)
-        self._dgrad(Ly["d2b"], g["d2b"], 32, 0, 1, g["d2a"], 32, 0)
-        self._relu_mask(a["d2a"], 32, 0, g["d2a"], 32, 0, 1, 32)
+        self._dgrad(Ly["d2b"], g["d2b"], 32, 0, 1, g["d2a"], 32, 0, mask=(a["d2a"], 32, 0))
         self._wgrad(Ly["d2a"], a["cat2"], 80, 0, g["d2a"], 32, 0, 1)
         self._dgrad(Ly["d2a"], g["d2a"], 32, 0, 1, g["cat2"], 80, 0)
-        self._up_bwd(g["cat2"], 80, 0, 2, 48, g["d3b"], 48, 0)
+        self._up_bwd(g["cat2"], 80, 0, 2, 48, g["d3b"], 48, 0, mask=(a["d3b"], 48, 0))
         # level 3 decoder
-        self._relu_mask(a["d3b"], 48, 0, g["d3b"], 48, 0, 2, 48)
         self._wgrad(Ly["d3b"], a["d3a"], 48, 0, g["d3b"], 48, 0, 2)
-        self._dgrad(Ly["d3b"], g["d3b"], 48, 0, 2, g["d3a"], 48, 0)
-        self._relu_mask(a["d3a"], 48, 0, g["d3a"], 48, 0, 2, 48)
+        self._dgrad(Ly["d3b"], g["d3b"], 48, 0, 2, g["d3a"], 48, 0, mask=(a["d3a"], 48, 0))
         self._wgrad(Ly["d3a"], a["cat3"], 112, 0, g["d3a"], 48, 0, 2)
         self._dgrad(Ly["d3a"], g["d3a"], 48, 0, 2, g["cat3"], 112, 0)
-        self._up_bwd(g["cat3"], 112, 0, 3, 64, g["b4b"], 64, 0)
+        self._up_bwd(g["cat3"], 112, 0, 3, 64, g["b4b"], 64, 0, mask=(a["b4b"], 64, 0))
         # bottom
-        self._relu_mask(a["b4b"], 64, 0, g["b4b"], 64, 0, 3, 64)
         self._wgrad(Ly["b4b"], a["b4a"], 64, 0, g["b4b"], 64, 0, 3)
-        self._dgrad(Ly["b4b"], g["b4b"], 64, 0, 3, g["b4a"], 64, 0)
-        self._relu_mask(a["b4a"], 64, 0, g["b4a"], 64, 0, 3, 64)
+        self._dgrad(Ly["b4b"], g["b4b"], 64, 0, 3, g["b4a"], 64, 0, mask=(a["b4a"], 64, 0))
         self._wgrad(Ly["b4a"], a["p3"], 48, 0, g["b4a"], 64, 0, 3)
         self._dgrad(Ly["b4a"], g["b4a"], 64, 0, 3, g["p3"], 48, 0)
         # level 3 encoder: skip gradient (cat3[64:112]) + pooling gradient
-        self._pool_bwd(g["p3"], 48, 0, 2, 48, g["cat3"], 112, 64, True)
-        self._relu_mask(a["cat3"], 112, 64, g["cat3"], 112, 64, 2, 48)
+        self._pool_bwd(g["p3"], 48, 0, 2, 48, g["cat3"], 112, 64, True, mask=(a["cat3"], 112, 64))
         self._wgrad(Ly["e3b"], a["e3a"], 48, 0, g["cat3"], 112, 64, 2)
-        self._dgrad(Ly["e3b"], g["cat3"], 112, 64, 2, g["e3a"], 48, 0)
-        self._relu_mask(a["e3a"], 48, 0, g["e3a"], 48, 0, 2, 48)
+        self._dgrad(Ly["e3b"], g["cat3"], 112, 64, 2, g["e3a"], 48, 0, mask=(a["e3a"], 48, 0))
         self._wgrad(Ly["e3a"], a["p2"], 32, 0, g["e3a"], 48, 0, 2)
         self._dgrad(Ly["e3a"], g["e3a"], 48, 0, 2, g["p2"], 32, 0)
         # level 2 encoder
-        self._pool_bwd(g["p2"], 32, 0, 1, 32, g["cat2"], 80, 48, True)
-        self._relu_mask(a["cat2"], 80, 48, g["cat2"], 80, 48, 1, 32)
+        self._pool_bwd(g["p2"], 32, 0, 1, 32, g["cat2"], 80, 48, True, mask=(a["cat2"], 80, 48))
         self._wgrad(Ly["e2b"], a["e2a"], 32, 0, g["cat2"], 80, 48, 1)
-        self._dgrad(Ly["e2b"], g["cat2"], 80, 48, 1, g["e2a"], 32, 0)
-        self._relu_mask(a["e2a"], 32, 0, g["e2a"], 32, 0, 1, 32)
+        self._dgrad(Ly["e2b"], g["cat2"], 80, 48, 1, g["e2a"], 32, 0, mask=(a["e2a"], 32, 0))
         self._wgrad(Ly["e2a"], a["p1"], 16, 0, g["e2a"], 32, 0, 1)
         self._dgrad(Ly["e2a"], g["e2a"], 32, 0, 1, g["p1"], 16, 0)
         # level 1 encoder
-        self._pool_bwd(g["p1"], 16, 0, 0, 16, g["cat1"], 48, 32, True)
-        self._relu_mask(a["cat1"], 48, 32, g["cat1"], 48, 32, 0, 16)
+        self._pool_bwd(g["p1"], 16, 0, 0, 16, g["cat1"], 48, 32, True, mask=(a["cat1"], 48, 32))
         self._wgrad(Ly["e1b"], a["e1a"], 16, 0, g["cat1"], 48, 32, 0)
-        self._dgrad(Ly["e1b"], g["cat1"], 48, 32, 0, g["e1a"], 16, 0)
-        self._relu_mask(a["e1a"], 16, 0, g["e1a"], 16, 0, 0, 16)
+        self._dgrad(Ly["e1b"], g["cat1"], 48, 32, 0, g["e1a"], 16, 0, mask=(a["e1a"], 16, 0))
         self._wgrad(Ly["e1a"], a["x0"], 8, 0, g["e1a"], 16, 0, 0)
+        # join: the main stream waits for the last weight gradient
+        e = self._event()
+        e.record(self.stream2)
+        self.stream.wait_event(e)
 
     def zero_grad(self):
         with self.torch.cuda.stream(self.stream):

@@ -95,6 +95,10 @@ def test_unet_calls_reject_null_operands(raw):
              "NULL")
     _rejects(L, L.sepx_unet_bias_grad(p, 12, 0, n(4), 8, p, None), "bad channel")
     _rejects(L, L.sepx_unet_adam_dev(p, p, p, p, n(8), None, None), "NULL")
+    assert L.sepx_unet_set_wgrad_form(3) == -1
+    _rejects(L, L.sepx_unet_pack_weights_many(65, p, p, p, p, p, p, None), "jobs")
+    _rejects(L, L.sepx_unet_pack_weights_many(2, None, p, p, p, p, p, None), "NULL")
+    assert L.sepx_unet_pack_weights_many(0, None, None, None, None, None, None, None) == 0
     _rejects(L, L.sepx_unet_adam_dev(p, p, p, p, n(-1), p, None), "n -1")
     assert L.sepx_unet_adam_dev(None, None, None, None, n(0), None, None) == 0
     _rejects(L, L.sepx_unet_capture_begin(None), "legacy stream")

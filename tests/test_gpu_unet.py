@@ -380,3 +380,73 @@ def test_network_speed(net):
         lib.sepx_unet_set_halo(prev)
     assert model.status() == 0
     print("UNET_NET " + json.dumps(res))
+
+
+@pytest.mark.parametrize("cin,cout,shape", [(16, 16, (2, 8, 16, 16)), (48, 64, (2, 4, 8, 8)),
+                                            (16, 1, (1, 4, 16, 16))])
+def test_fused_relu_backward_is_bit_identical(net, cin, cout, shape):
+    """The ReLU backward fused into the data gradient, the pooling gradient
+    and the upsampling gradient gives the same bits as the separate
+    relu_mask pass after them."""
+    from sep_code_gb300._lib import lib
+    lib.sepx_setup_cuda(1)
+    st = lib.sepx_get_stream()
+    rng = np.random.default_rng(cin + cout)
+    nb, D, H, W = shape
+    ntap = 1 if cout == 1 else 27
+    cin_p, cout_p = (cin + 7) // 8 * 8, (cout + 7) // 8 * 8
+    V = nb * D * H * W
+    w = (rng.standard_normal((ntap, cin_p, cout)) / np.sqrt(ntap * cin)).astype(np.float32)
+    wt = torch.tensor(w).cuda()
+    pkt = torch.zeros(net.lib.sepx_unet_packed_elems(cout, cin_p, ntap, 1), dtype=torch.bfloat16).cuda()
+    torch.cuda.synchronize()
+    net._chk(net.lib.sepx_unet_pack_weights(net._p(wt), cout, cin_p, ntap, 1, net._p(pkt), st))
+    dy = np.zeros((V, cout_p))
+    dy[:, :cout] = U.bf16(rng.standard_normal((V, cout)))
+    act = U.bf16(rng.standard_normal((V, cin_p + 8)))   # mask view: channels 8 .. 8 + cin_p
+    dyt, actt = _bf(dy), _bf(act)
+    outs = []
+    for fused in (True, False):
+        dx = torch.zeros((V, cin_p), dtype=torch.bfloat16).cuda()
+        torch.cuda.synchronize()
+        m = (net._p(actt), cin_p + 8, 8) if fused else (None, 0, 0)
+        net._chk(net.lib.sepx_unet_conv_fwd_masked(net._p(dyt), cout_p, 0, nb, D, H, W, cout_p, ntap,
+                                                   net._p(pkt), None, cin_p, 0, net._p(dx), cin_p, 0,
+                                                   None, None, *m, st))
+        if not fused:
+            net._chk(net.lib.sepx_unet_relu_mask(net._p(actt), cin_p + 8, 8, net._p(dx), cin_p, 0, V, cin_p, st))
+        _sync(net)
+        outs.append(dx.view(torch.int16).cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert (outs[0] == 0).mean() > 0.3   # the mask did zero about half
+    # pooling gradient (accumulating into a slice) and upsampling gradient
+    C = cin_p
+    g2 = _bf(U.bf16(rng.standard_normal((V // 8, C))))
+    base = U.bf16(rng.standard_normal((V, 2 * C)))
+    res = []
+    for fused in (True, False):
+        dst = _bf(base)
+        torch.cuda.synchronize()
+        m = (net._p(actt), cin_p + 8, 8) if fused else (None, 0, 0)
+        net._chk(net.lib.sepx_unet_avgpool_bwd_masked(net._p(g2), C, 0, nb, D, H, W, C, net._p(dst), 2 * C, C,
+                                                      1, *m, st))
+        if not fused:
+            net._chk(net.lib.sepx_unet_relu_mask(net._p(actt), cin_p + 8, 8, net._p(dst), 2 * C, C, V, C, st))
+        _sync(net)
+        res.append(dst.view(torch.int16).cpu().numpy())
+    assert np.array_equal(res[0], res[1])
+    fine = _bf(U.bf16(rng.standard_normal((V, C))))
+    act2 = _bf(U.bf16(rng.standard_normal((V // 8, C))))
+    res = []
+    for fused in (True, False):
+        dx = torch.zeros((V // 8, C), dtype=torch.bfloat16).cuda()
+        torch.cuda.synchronize()
+        m = (net._p(act2), C, 0) if fused else (None, 0, 0)
+        net._chk(net.lib.sepx_unet_upsample_bwd_masked(net._p(fine), C, 0, nb, D // 2, H // 2, W // 2, C,
+                                                       net._p(dx), C, 0, *m, st))
+        if not fused:
+            net._chk(net.lib.sepx_unet_relu_mask(net._p(act2), C, 0, net._p(dx), C, 0, V // 8, C, st))
+        _sync(net)
+        res.append(dx.view(torch.int16).cpu().numpy())
+    assert np.array_equal(res[0], res[1])
+    assert net.lib.sepx_unet_status() == 0

@@ -1,5 +1,6 @@
-"""The tap-stacked TMA weight gradient (csrc/sepx_unet_wgrad.inc) against the
-FP64 restatement (oracle/unet_oracle.py) and the per-tap gather kernel.
+"""The tap-stacked weight gradients (csrc/sepx_unet_wgrad.inc: the z-walk
+form and the per-tile form) against the FP64 restatement
+(oracle/unet_oracle.py) and the per-tap gather kernel.
 
 Shapes: every (cin, cout) of the U-Net that takes the kernel (cout <= 40,
 cin <= 80), ragged planes (H not a multiple of 16, W not a multiple of 8),
@@ -29,6 +30,9 @@ CASES = [
     (48, 16, 1, 2, 32, 16, (48, 0), (48, 32)),
     (80, 32, 1, 3, 16, 16, (80, 0), (32, 0)),
     (24, 40, 1, 1, 7, 5, (24, 0), (40, 0)),
+    # several windows along z per volume
+    (16, 16, 2, 40, 16, 16, (16, 0), (16, 0)),
+    (48, 16, 1, 33, 16, 24, (48, 0), (16, 0)),
 ]
 
 
@@ -80,19 +84,22 @@ def test_wgrad_bias_against_fp64_and_gather(unet, cin, cout, nb, D, H, W, xs, ds
     db0 = np.full(cout, -0.5, np.float32)
     want_dw = U.conv_wgrad(x, dy[..., :cout], 27, cin).ravel() + 0.25
     want_db = dy[..., :cout].sum((0, 1, 2, 3)) - 0.5
-    dw, db = _run(unet, xt, xs, dyt, ds, cin, cout, nb, D, H, W, dw0, db0)
-    e_w, e_b = rel_l2(dw, want_dw), rel_l2(db, want_db)
-    dw2, db2 = _run(unet, xt, xs, dyt, ds, cin, cout, nb, D, H, W, dw0, db0)
-    prev = lib.sepx_unet_set_halo(0)
-    try:
-        gw, gb = _run(unet, xt, xs, dyt, ds, cin, cout, nb, D, H, W, dw0, db0)
-    finally:
-        lib.sepx_unet_set_halo(prev)
-    print(f"WGRAD_TMA cin {cin} cout {cout} {nb}x{D}x{H}x{W}: dw rel-L2 {e_w:.2e}, db {e_b:.2e}, "
-          f"vs gather {rel_l2(dw, gw):.2e}, repeatable {np.array_equal(dw, dw2) and np.array_equal(db, db2)}")
-    assert e_w <= 1e-5 and e_b <= 1e-5, (e_w, e_b)
-    assert rel_l2(gw, want_dw) <= 1e-5 and rel_l2(gb, want_db) <= 1e-5
-    assert np.array_equal(dw, dw2) and np.array_equal(db, db2)
+    res = {}
+    for form in (2, 1, 0):
+        prev = lib.sepx_unet_set_wgrad_form(form)
+        try:
+            dw, db = _run(unet, xt, xs, dyt, ds, cin, cout, nb, D, H, W, dw0, db0)
+            dw2, db2 = _run(unet, xt, xs, dyt, ds, cin, cout, nb, D, H, W, dw0, db0)
+        finally:
+            lib.sepx_unet_set_wgrad_form(prev)
+        e_w, e_b = rel_l2(dw, want_dw), rel_l2(db, want_db)
+        same = np.array_equal(dw, dw2) and np.array_equal(db, db2)
+        res[form] = (e_w, e_b, same)
+        assert e_w <= 1e-5 and e_b <= 1e-5, (form, e_w, e_b)
+        if form > 0:   # the tap-stacked forms add their partials in a fixed order
+            assert same, form
+    print(f"WGRAD_TMA cin {cin} cout {cout} {nb}x{D}x{H}x{W}: (dw rel-L2, db rel-L2, repeatable) "
+          f"z-walk {res[2]}, per-tile {res[1]}, gather {res[0]}")
 
 
 def test_bias_grad_kernel(unet):
