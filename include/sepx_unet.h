@@ -68,9 +68,8 @@ int sepx_unet_conv_wgrad(const void *x, int x_cstride, int x_coff, int nb, int D
 /* The same, plus db[cout] += sum_v dy[v][cout] when db is not NULL (taken
  * from the same tiles on the tap-stacked kernel).  The tap-stacked kernel
  * sums per-CTA partials in a fixed order (repeatable results); it keeps them
- * in a library scratch buffer (one for the gradient sums, one for the split-K
- * convolutions), so weight gradients on two streams must not overlap, and the
- * first call of a shape must not be inside a graph capture. */
+ * in a library scratch buffer per stream (up to 16 streams), grown on demand:
+ * the first call of a shape on a stream must not be inside a graph capture. */
 int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, int D, int H, int W,
                               int cin, int ntap, const void *dy, int dy_cstride, int dy_coff, int cout,
                               float *dw, float *db, void *stream);

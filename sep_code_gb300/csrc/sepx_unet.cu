@@ -1284,28 +1284,41 @@ int encode_view(CUtensorMap *tm, const void *p, int cstride, int coff, int chans
 }
 
 // Device scratch for partial sums, grown on demand (a call inside a CUDA-graph
-// capture must not grow it: run the sequence once before capturing).  Two
-// pools: kScrConv for the split-K convolutions, kScrGrad for the weight and
-// bias gradients -- so that the two kinds may run on different streams
-// (the training step runs its weight gradients beside the data gradients).
+// capture must not grow it: run the sequence once before capturing).  One
+// buffer per (pool, stream) -- kScrConv for the split-K convolutions,
+// kScrGrad for the weight and bias gradients -- so that calls on different
+// streams never share one (the training step runs its weight gradients on
+// streams beside the data gradients).
 enum { kScrConv = 0, kScrGrad = 1 };
-float *g_scratch[2] = {nullptr, nullptr};
-size_t g_scratch_floats[2] = {0, 0};
-int unet_scratch(int pool, size_t floats, float **p) {
-  if (floats > g_scratch_floats[pool]) {
+struct Scratch {
+  cudaStream_t st;
+  float *p;
+  size_t n;
+};
+constexpr int kMaxScratch = 16;
+Scratch g_scratch[2][kMaxScratch] = {};
+int unet_scratch(int pool, size_t floats, float **p, cudaStream_t st) {
+  Scratch *e = nullptr;
+  for (int i = 0; i < kMaxScratch && !e; i++)
+    if (g_scratch[pool][i].p && g_scratch[pool][i].st == st) e = &g_scratch[pool][i];
+  for (int i = 0; i < kMaxScratch && !e; i++)
+    if (!g_scratch[pool][i].p) e = &g_scratch[pool][i];
+  if (!e) return set_error("unet: more than %d streams use the scratch buffers", kMaxScratch);
+  if (floats > e->n || !e->p) {
     float *q = nullptr;
-    if (cudaMalloc((void **)&q, floats * sizeof(float)) != cudaSuccess) {
+    if (cudaMalloc((void **)&q, std::max<size_t>(floats, 1) * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
       return set_error("unet: cannot allocate %zu floats of scratch", floats);
     }
-    if (g_scratch[pool]) {
+    if (e->p) {
       cudaDeviceSynchronize();   // nothing may still read the old buffer
-      cudaFree(g_scratch[pool]);
+      cudaFree(e->p);
     }
-    g_scratch[pool] = q;
-    g_scratch_floats[pool] = floats;
+    e->p = q;
+    e->n = std::max<size_t>(floats, 1);
+    e->st = st;
   }
-  *p = g_scratch[pool];
+  *p = e->p;
   return 0;
 }
 
@@ -1433,7 +1446,7 @@ int conv_wgrad_zw(const void *x, int x_cstride, int x_coff, int nb, int D, int H
     return -1;
   const long long n = 27LL * cin * cout;
   float *scr;
-  if (unet_scratch(kScrGrad, (size_t)grid * (size_t)(n + cout), &scr)) return -1;
+  if (unet_scratch(kScrGrad, (size_t)grid * (size_t)(n + cout), &scr, st)) return -1;
   a.part = scr;
   a.bpart = scr + (size_t)grid * n;
   conv_wgrad_zw_kernel<<<(unsigned)grid, kZwThreads, smem, st>>>(tmx, tmy, a);
@@ -1513,7 +1526,7 @@ int conv_wgrad_tma(const void *x, int x_cstride, int x_coff, int nb, int D, int 
   a.mrows = 3 * 8 * ngo <= 64 ? 64 : 128;
   const long long n = 27LL * cin * cout;
   float *scr;
-  if (unet_scratch(kScrGrad, (size_t)a.groups * (size_t)(n + cout), &scr)) return -1;
+  if (unet_scratch(kScrGrad, (size_t)a.groups * (size_t)(n + cout), &scr, st)) return -1;
   a.part = scr;
   a.bpart = scr + (size_t)a.groups * n;
   conv_wgrad_tma_kernel<<<(unsigned)(a.groups * nzg), kWgThreads, smem, st>>>(tmx, tmy, a);
@@ -1532,7 +1545,7 @@ int bias_grad(const void *dy, int dy_cstride, int dy_coff, long long V, int c, f
   long long blocks = (V + lanes - 1) / lanes;
   if (blocks > 2 * 152) blocks = 2 * 152;
   float *scr;
-  if (unet_scratch(kScrGrad, (size_t)blocks * c, &scr)) return -1;
+  if (unet_scratch(kScrGrad, (size_t)blocks * c, &scr, st)) return -1;
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
   bias_grad_kernel<<<(unsigned)blocks, kBiasThreads, 0, st>>>(dv, V, c, scr);
   bias_sum_kernel<<<(c + 3) / 4, 128, 0, st>>>(scr, (int)blocks, c, db);
@@ -1682,7 +1695,7 @@ int sepx_unet_conv_fwd_masked(const void *x, int x_cstride, int x_coff, int nb, 
   }
   if (splits > 1) {
     float *kpart;
-    if (unet_scratch(kScrConv, (size_t)splits * V * np, &kpart)) return -1;
+    if (unet_scratch(kScrConv, (size_t)splits * V * np, &kpart, (cudaStream_t)stream)) return -1;
     conv_fwd_kernel<<<dim3((unsigned)mt, (unsigned)splits), kUThreads, smem, (cudaStream_t)stream>>>(
         xv, nb, D, H, W, cin, ntap, (const __nv_bfloat16 *)wpacked, kch, bias, cout, np, relu,
         (__nv_bfloat16 *)y, y_cstride, y_coff, yf, resid, err, kper, kpart, mv);
@@ -1733,7 +1746,7 @@ int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, 
     constexpr int NP = 16 * 1 + 1;
     const long long blocks = std::min<long long>((V + 255) / 256, 2 * 152);
     float *scr;
-    if (unet_scratch(kScrGrad, (size_t)blocks * NP, &scr)) return -1;
+    if (unet_scratch(kScrGrad, (size_t)blocks * NP, &scr, (cudaStream_t)stream)) return -1;
     View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
     View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
     float *bscr = scr + (size_t)blocks * 16;

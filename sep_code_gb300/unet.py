@@ -126,7 +126,7 @@ class UNet3D:
     """Device-resident network: parameters, Adam state and activation buffers
     (allocated per input shape).  All work is enqueued on the library stream."""
 
-    def __init__(self, params: dict | None = None, seed: int = 0):
+    def __init__(self, params: dict | None = None, seed: int = 0, grad_streams: int = 2):
         import torch
         self.torch = torch
         self.dev = torch.device("cuda")
@@ -166,13 +166,13 @@ class UNet3D:
         self.step_count = 0
         self.shape = None
         self.graph, self.graph_io = None, None
-        # the weight gradients run on a second stream beside the data
-        # gradients (each forks from the main stream once its dy is ready; the
-        # main stream joins it at the end of the backward pass)
-        self.stream2 = torch.cuda.Stream(device=self.dev)
-        self.stream2_ptr = C.c_void_p(self.stream2.cuda_stream)
-        self._events = [torch.cuda.Event() for _ in range(len(LAYERS) + 1)]
+        # the weight gradients run on side streams beside the data gradients,
+        # taken in turn (each forks from the main stream once its dy is ready;
+        # the main stream joins them at the end of the backward pass)
+        self.grad_streams = [torch.cuda.Stream(device=self.dev) for _ in range(grad_streams)]
+        self._events = [torch.cuda.Event() for _ in range(len(LAYERS) + grad_streams)]
         self._nev = 0
+        self._ngs = 0
         self.pack()
 
     # ---------------------------------------------------------------- params
@@ -276,12 +276,14 @@ class UNet3D:
         main stream has enqueued so far (dy is ready there)"""
         nb = self.shape[0]
         D, H, W = self.dims[lvl]
+        gs = self.grad_streams[self._ngs % len(self.grad_streams)]
+        self._ngs += 1
         e = self._event()
         e.record(self.stream)
-        self.stream2.wait_event(e)
+        gs.wait_event(e)
         _chk(lib.sepx_unet_conv_wgrad_bias(_p(x), xcs, xco, nb, D, H, W, L.cin_p, L.ntap, _p(dy), dycs,
                                            dyco, L.cout, _p(self.gw[L.name]), _p(self.gb[L.name]),
-                                           self.stream2_ptr))
+                                           C.c_void_p(gs.cuda_stream)))
 
     def _relu_mask(self, y, ycs, yco, dy, dycs, dyco, lvl, c):
         _chk(lib.sepx_unet_relu_mask(_p(y), ycs, yco, _p(dy), dycs, dyco, self.V[lvl], c,
@@ -398,10 +400,12 @@ class UNet3D:
         self._wgrad(Ly["e1b"], a["e1a"], 16, 0, g["cat1"], 48, 32, 0)
         self._dgrad(Ly["e1b"], g["cat1"], 48, 32, 0, g["e1a"], 16, 0, mask=(a["e1a"], 16, 0))
         self._wgrad(Ly["e1a"], a["x0"], 8, 0, g["e1a"], 16, 0, 0)
-        # join: the main stream waits for the last weight gradient
-        e = self._event()
-        e.record(self.stream2)
-        self.stream.wait_event(e)
+        # join: the main stream waits for the weight gradients
+        for gs in self.grad_streams:
+            e = self._event()
+            e.record(gs)
+            self.stream.wait_event(e)
+        self._ngs = 0
 
     def zero_grad(self):
         with self.torch.cuda.stream(self.stream):
@@ -536,10 +540,12 @@ def main(argv=None):
     p.add_argument("--gather", action="store_true", help="use the per-tap gather kernel")
     p.add_argument("--train-steps", type=int, default=0,
                    help="instead: time this many Adam training steps on a batch of nb x n^3")
+    p.add_argument("--grad-streams", type=int, default=2,
+                   help="side streams for the weight gradients of the training step")
     a = p.parse_args(argv)
     if a.train_steps > 0:
         import torch
-        model = UNet3D(seed=3)
+        model = UNet3D(seed=3, grad_streams=a.grad_streams)
         g = torch.Generator(device="cuda").manual_seed(9)
         x = torch.randn(a.nb, a.n, a.n, a.n, device="cuda", generator=g)
         t = torch.randn(a.nb, a.n, a.n, a.n, device="cuda", generator=g)
