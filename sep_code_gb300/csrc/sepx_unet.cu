@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
     View x, int nb, int D, int H, int W, int cin, int ntap, View dy, int cout, int np,
-    int vchunks_per_cta, float *dw, int *err) {
+    int vchunks_per_cta, float *dw, int *err, float *part) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -775,7 +775,11 @@ __global__ void __launch_bounds__(kUThreads) conv_wgrad_kernel(
       if (m < mtot) {
 #pragma unroll
         for (int i = 0; i < 16; i++)
-          if (n0 + i < cout) atomicAdd(dw + (size_t)m * cout + n0 + i, acc[i]);
+          if (n0 + i < cout) {
+            // part: this split's sums, added in split order by wg_reduce_kernel
+            if (part) part[((size_t)blockIdx.y * mtot + m) * cout + n0 + i] = acc[i];
+            else atomicAdd(dw + (size_t)m * cout + n0 + i, acc[i]);
+          }
       }
     }
   }
@@ -1764,6 +1768,17 @@ int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, 
   // split adds its sums with FP32 atomics, so more splits cost contention
   long long per = (vchunks * mt + 2 * 152 * 4 - 1) / (2 * 152 * 4);
   per = std::max(per, std::max(4LL, std::min(16LL, vchunks / 8)));
+  // with the halo-staged kernels on, each split writes its sums to a partial
+  // buffer that wg_reduce_kernel adds in split order (repeatable bits, no
+  // atomics); at least 8 voxel chunks per split keep the partials small
+  float *part = nullptr;
+  const long long mtot = (long long)ntap * cin;
+  if (g_halo_enabled) {
+    per = std::max(per, 8LL);
+    while ((vchunks + per - 1) / per * mtot * cout > (16LL << 20)) per *= 2;
+    if (unet_scratch(kScrGrad, (size_t)((vchunks + per - 1) / per * mtot * cout), &part, (cudaStream_t)stream))
+      return -1;
+  }
   const long long splits = (vchunks + per - 1) / per;
   const size_t smem = conv_smem(np);
   static bool attr = false;
@@ -1776,7 +1791,12 @@ int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, 
   View xv{(const __nv_bfloat16 *)x, x_cstride, x_coff};
   View dv{(const __nv_bfloat16 *)dy, dy_cstride, dy_coff};
   conv_wgrad_kernel<<<dim3(mt, (unsigned)splits), kUThreads, smem, (cudaStream_t)stream>>>(
-      xv, nb, D, H, W, cin, ntap, dv, cout, np, (int)per, dw, err);
+      xv, nb, D, H, W, cin, ntap, dv, cout, np, (int)per, dw, err, part);
+  if (part) {
+    const long long n = mtot * cout;
+    wg_reduce_kernel<<<(unsigned)((n + 31) / 32), 32 * kRedSlices, 0, (cudaStream_t)stream>>>(
+        part, (int)splits, n, dw, nullptr, 0, nullptr);
+  }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : set_error("unet wgrad: %s", cudaGetErrorString(e));
 }

@@ -8,8 +8,8 @@ an x view and a dy view that are channel slices of wider buffers, volumes
 with one plane.  dw and db are added to what they hold.
 
 Tolerance: relative L2 <= 1e-5 against the FP64 sums of the same BF16
-operands (FP32 accumulation in a different order).  The kernel adds its CTAs'
-partial sums in a fixed order, so two runs give identical bits.
+operands (FP32 accumulation in a different order).  Every form adds its
+CTAs' partial sums in a fixed order, so two runs give identical bits.
 """
 import numpy as np
 import pytest
@@ -96,8 +96,7 @@ def test_wgrad_bias_against_fp64_and_gather(unet, cin, cout, nb, D, H, W, xs, ds
         same = np.array_equal(dw, dw2) and np.array_equal(db, db2)
         res[form] = (e_w, e_b, same)
         assert e_w <= 1e-5 and e_b <= 1e-5, (form, e_w, e_b)
-        if form > 0:   # the tap-stacked forms add their partials in a fixed order
-            assert same, form
+        assert same, form   # every form adds its partial sums in a fixed order
     print(f"WGRAD_TMA cin {cin} cout {cout} {nb}x{D}x{H}x{W}: (dw rel-L2, db rel-L2, repeatable) "
           f"z-walk {res[2]}, per-tile {res[1]}, gather {res[0]}")
 
