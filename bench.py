@@ -44,6 +44,8 @@ def parse_args():
     # 25 steps of each loop on the full grid: about 13 s of CPU work on 16 cores
     p.add_argument("--cpu-sample-steps", type=int, default=25)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--e2e-clock-ms", type=int, default=1000,
+                   help="nvidia-smi sampling interval during the e2e region (0: none)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", default="rtm", choices=["rtm", "batch"],
                    help="rtm: the single-shot RTM line; batch: 16 batched shots")
@@ -374,13 +376,14 @@ def run_ours(args, ws, rank, dist):
         # one sample a second here: polling every 200 ms slowed the host-buffer
         # Born forward of this step by 0.4-0.5 s (8.50 -> 8.95-9.15 s per step,
         # the device-resident loops were unaffected)
-        e2e_clocks = ClockSampler(interval_ms=1000)
-        e2e_clocks.start()
+        e2e_clocks = ClockSampler(interval_ms=args.e2e_clock_ms) if args.e2e_clock_ms > 0 else None
+        if e2e_clocks:
+            e2e_clocks.start()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             e2e_step()
         e_el = max_over_ranks(dist, time.perf_counter() - t0)
-        e2e_clk = e2e_clocks.stop()
+        e2e_clk = e2e_clocks.stop() if e2e_clocks else None
         vb = 4 * n1 * n2 * n3
         tb = 4 * nrec * st.nt_big
         h2d = 3 * vb + vb + 2 * vb + 2 * tb + 4 * (h_v9.size + 2 * h_v8.size)
