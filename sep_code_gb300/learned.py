@@ -135,6 +135,12 @@ def train(net: UNet3D, X, Y, epochs: int = 10, batch: int = 4, lr: float = 1e-3,
     net.stream.synchronize()
     hist = []
     n = len(X)
+    # fixed batch buffers: the first step is captured into a CUDA graph
+    # (UNet3D.capture_train_step) and every later step replays it
+    with torch.cuda.stream(net.stream):
+        xb = torch.empty((batch,) + tuple(Xd.shape[1:]), dtype=Xd.dtype, device="cuda")
+        yb = torch.empty((batch,) + tuple(Yd.shape[1:]), dtype=Yd.dtype, device="cuda")
+    captured = False
     for ep in range(epochs):
         order = rng.permutation(n)
         lr_ep = lr * (0.5 * (1 + np.cos(np.pi * ep / max(epochs, 1))))   # cosine decay
@@ -143,9 +149,16 @@ def train(net: UNet3D, X, Y, epochs: int = 10, batch: int = 4, lr: float = 1e-3,
         for i in range(0, n - batch + 1, batch):
             idx = torch.tensor(order[i:i + batch], device="cuda")
             with torch.cuda.stream(net.stream):
-                xb = Xd.index_select(0, idx)
-                yb = Yd.index_select(0, idx)
-            tot += net.train_step(xb, yb, lr=max(lr_ep, lr * 0.02))
+                torch.index_select(Xd, 0, idx, out=xb)
+                torch.index_select(Yd, 0, idx, out=yb)
+            step_lr = max(lr_ep, lr * 0.02)
+            if not captured:
+                net.capture_train_step(xb, yb, lr=step_lr)   # trains on this batch once
+                net.stream.synchronize()
+                tot += float(net.loss.item())
+                captured = True
+            else:
+                tot += net.train_step(xb, yb, lr=step_lr)
             nb += 1
         hist.append(tot / max(nb, 1))
         if verbose:

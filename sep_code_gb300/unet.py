@@ -454,14 +454,14 @@ class UNet3D:
         self.stream.synchronize()
         return float(self.loss.item())
 
-    def capture_train_step(self, x, target):
+    def capture_train_step(self, x, target, lr=1e-3):
         """Capture one whole training step (gradient zeroing, forward, loss,
         backward, Adam, weight packing: about 140 launches) into a CUDA graph
         that reads its batch from x and target; train_step on these same
         tensors then replays it with one launch.  Runs one eager step first
         (buffer allocation, kernel attributes), which trains the network on
         this batch once."""
-        self.train_step(x, target)
+        self.train_step(x, target, lr=lr)
         self.free_graph()
         self.stream.synchronize()
         _chk(lib.sepx_unet_capture_begin(self.stream_ptr))

@@ -450,3 +450,38 @@ def test_fused_relu_backward_is_bit_identical(net, cin, cout, shape):
         res.append(dx.view(torch.int16).cpu().numpy())
     assert np.array_equal(res[0], res[1])
     assert net.lib.sepx_unet_status() == 0
+
+
+def test_learned_train_loop_replays_the_captured_step(net):
+    """learned.train: fixed batch buffers, the first step captured into a
+    graph and replayed for the others; on a fixed smoothing task the epoch
+    losses fall, and the weights equal those of the same steps launched one
+    by one to summation-order noise."""
+    from sep_code_gb300 import learned
+    rng = np.random.default_rng(12)
+    n, D = 8, 16
+    X = rng.standard_normal((n, D, D, D)).astype(np.float32)
+    Y = X.copy()
+    for ax in (1, 2, 3):
+        Y = (np.roll(Y, 1, ax) + 2 * Y + np.roll(Y, -1, ax)) / 4
+    Y = Y.astype(np.float32)
+    m1 = net.UNet3D(seed=2)
+    hist = learned.train(m1, X, Y, epochs=4, batch=2, lr=2e-3, seed=1)
+    assert m1.graph is not None and m1.status() == 0
+    assert all(np.isfinite(hist)) and hist[-1] < hist[0], hist
+    # the same schedule, every step launched one by one
+    m2 = net.UNet3D(seed=2)
+    r = np.random.default_rng(1)
+    Xd, Yd = torch.tensor(X).cuda(), torch.tensor(Y).cuda()
+    for ep in range(4):
+        order = r.permutation(n)
+        lr_ep = 2e-3 * (0.5 * (1 + np.cos(np.pi * ep / 4)))
+        for i in range(0, n - 1, 2):
+            idx = torch.tensor(order[i:i + 2], device="cuda")
+            xb, yb = Xd.index_select(0, idx).contiguous(), Yd.index_select(0, idx).contiguous()
+            torch.cuda.synchronize()
+            m2.train_step(xb, yb, lr=max(lr_ep, 2e-3 * 0.02))
+    for L in net.LAYERS:
+        a, b = m1.w[L.name].cpu().numpy(), m2.w[L.name].cpu().numpy()
+        assert rel_l2(a, b) <= 1e-3, (L.name, rel_l2(a, b))
+    m1.free_graph()
