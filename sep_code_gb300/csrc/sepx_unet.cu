@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "sepx_common.h"
 #include "sepx_device.cuh"
@@ -1301,7 +1302,9 @@ struct Scratch {
 };
 constexpr int kMaxScratch = 16;
 Scratch g_scratch[2][kMaxScratch] = {};
+std::mutex g_scratch_mu;   // host threads may enqueue on different streams
 int unet_scratch(int pool, size_t floats, float **p, cudaStream_t st) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
   Scratch *e = nullptr;
   for (int i = 0; i < kMaxScratch && !e; i++)
     if (g_scratch[pool][i].p && g_scratch[pool][i].st == st) e = &g_scratch[pool][i];
