@@ -333,10 +333,10 @@ def main(argv=None):
     p = argparse.ArgumentParser(description="train the U-Net preconditioner / compare LSRTM")
     sub = p.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train")
-    t.add_argument("--pairs", type=int, default=2000)
+    t.add_argument("--pairs", type=int, default=4000)
     t.add_argument("--n", type=int, default=64)
     t.add_argument("--nt", type=int, default=1100)
-    t.add_argument("--epochs", type=int, default=12)
+    t.add_argument("--epochs", type=int, default=24)
     t.add_argument("--batch", type=int, default=4)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--out", default=str(WEIGHTS))

@@ -1,6 +1,6 @@
 """What the trained U-Net preconditioner buys inside least-squares RTM.
 
-The committed network (sep_code_gb300/data/unet_precond.npz, trained on 2000
+The committed network (sep_code_gb300/data/unet_precond.npz, trained on 4000
 64^3 pairs (L'L m, m) of the Born operator) preconditions the search
 direction of simple_solver + cgstep; plain CG runs on the same operator and
 data.  On an unseen survey the learned direction must reach plain CG's final
