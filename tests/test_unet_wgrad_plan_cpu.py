@@ -7,7 +7,8 @@ refilled only after its plane's last tile), the partial layout -- against
 the direct sum dW[t][c][m] = sum_u dY[u][m] X[u + off(t)][c] and db.  Also
 the shared-memory and tensor-memory plans of every U-Net layer shape that
 takes these kernels, as the host code sizes them (227 KB per CTA, 512
-columns per SM, the A view of 64 or 128 rows inside the carve).
+columns per SM, the A view of 64 or 128 rows inside the carve), and the
+K-chunk walk of the split-K gather convolution.
 """
 import numpy as np
 import pytest
@@ -231,3 +232,33 @@ def test_pertile_schedule_gives_the_weight_gradient(cin, cout, ndz):
     dw, db = pertile_emulate(x, dy, cin, cout, ndz, groups=3)
     w2, b2 = direct(x, dy, cin, cout)
     assert np.abs(dw - w2).max() < 1e-9 and np.abs(db - b2).max() < 1e-9
+
+
+def test_split_k_chunk_positions_cover_every_tap_and_channel_once():
+    """conv_fwd_kernel's split K: split k sums K chunks [k*kper, (k+1)*kper)
+    of 64 (8 groups of 8 channels), starting at tap (kb*64)/cin and channel
+    (kb*64)%cin and stepping 8 channels at a time (next tap at cin).  Every
+    (tap, channel group) is visited by exactly one split, in K order."""
+    KKC = 64
+    for cin in (8, 16, 32, 48, 64, 80, 112):
+        for ntap in (1, 27):
+            kch = (ntap * cin + KKC - 1) // KKC
+            mt = 16
+            splits = min((2 * 152 + mt - 1) // mt, kch // 2) if kch >= 4 else 1
+            kper = (kch + splits - 1) // splits
+            splits = (kch + kper - 1) // kper
+            seen = []
+            for k in range(splits):
+                kb = k * kper
+                nk = min(kper, kch - kb)
+                tap, c0 = (kb * KKC) // cin, (kb * KKC) % cin
+                for _ in range(nk):
+                    for _ in range(KKC // 8):
+                        if tap < ntap:
+                            seen.append((tap, c0))
+                        c0 += 8
+                        if c0 >= cin:
+                            c0 -= cin
+                            tap += 1
+            want = [(t, c) for t in range(ntap) for c in range(0, cin, 8)]
+            assert seen == want, (cin, ntap)
