@@ -428,14 +428,18 @@ __global__ void __launch_bounds__(kHaloThreads) conv_halo_kernel(const __grid_co
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
 
+  // tile indices fit 32 bits (volumes hold fewer than 2^31 voxels): 32-bit
+  // divisions, several times cheaper than 64-bit ones in the issuing lanes
   auto tile_pos = [&](int k, int &n, int &z, int &y0, int &x0) {
-    const long long tile = blockIdx.x + (long long)k * gridDim.x;
-    const int bx = (int)(tile % a.tx);
-    long long r = tile / a.tx;
-    const int by = (int)(r % a.ty);
-    r /= a.ty;
-    z = (int)(r % a.D);
-    n = (int)(r / a.D);
+    const uint32_t tile = blockIdx.x + (uint32_t)k * gridDim.x;
+    const uint32_t tx = (uint32_t)a.tx, ty = (uint32_t)a.ty, dd = (uint32_t)a.D;
+    uint32_t r = tile / tx;
+    const int bx = (int)(tile - r * tx);
+    const uint32_t r2 = r / ty;
+    const int by = (int)(r - r2 * ty);
+    const uint32_t r3 = r2 / dd;
+    z = (int)(r2 - r3 * dd);
+    n = (int)r3;
     y0 = by * kTileY;
     x0 = bx * kTileX;
   };
@@ -1343,6 +1347,7 @@ int conv_halo(const void *x, int x_cstride, int x_coff, int nb, int D, int H, in
   a.ty = (H + kTileY - 1) / kTileY;
   a.tx = (W + kTileX - 1) / kTileX;
   a.ntiles = (long long)nb * D * a.ty * a.tx;
+  if (a.ntiles >= (1LL << 31)) return set_error("unet conv: too many tiles");
   a.wbytes = wbytes;
   // resident CTAs per SM from the shared memory each needs (the CTAs of the
   // persistent grid must all be resident): two halo buffers unless one
@@ -1444,6 +1449,7 @@ int conv_wgrad_zw(const void *x, int x_cstride, int x_coff, int nb, int D, int H
     if (zc <= 4) break;
   }
   a.nitems = cols * a.nzc;
+  if (a.nitems >= (1LL << 31)) return 1;
   const long long grid = a.nitems < slots ? a.nitems : slots;
   a.err = err;
   a.mrows = 3 * 8 * ngo <= 64 ? 64 : 128;
@@ -1522,6 +1528,7 @@ int conv_wgrad_tma(const void *x, int x_cstride, int x_coff, int nb, int D, int 
   a.ty = (H + 15) / 16;
   a.tx = (W + 2 + 7) / 8;
   a.ntiles = (long long)nb * D * a.ty * a.tx;
+  if (a.ntiles >= (1LL << 31)) return 1;
   a.groups = (g_num_sms * per_sm) / nzg;
   if (a.groups > a.ntiles) a.groups = (int)a.ntiles;
   if (a.groups < 1) a.groups = 1;
