@@ -11,6 +11,19 @@
 
 namespace sepx {
 
+// q = k / d, r = k % d with 32-bit division when the walk is shorter than 2^31
+// (uniform per launch); 64-bit divisions otherwise.  Index arithmetic only.
+__device__ __forceinline__ long long divmod(long long k, int d, bool narrow, int &rem) {
+  if (narrow) {
+    const uint32_t q = (uint32_t)k / (uint32_t)d;
+    rem = (int)((uint32_t)k - q * (uint32_t)d);
+    return q;
+  }
+  const long long q = k / d;
+  rem = (int)(k - q * d);
+  return q;
+}
+
 // img_pad = laplac::forward(extract_sub(model))  (Born/image_rtm_3d.cpp:52-90,
 // Born/laplac_3d.cpp:46-96 with a unit mute): e(z) = model[z+f] (0 outside),
 // d(0) = -e(0), d(z) = e(z-1) - e(z) for 0 < z < n3-1, d(n3-1) = e(n3-2).
@@ -18,9 +31,11 @@ __global__ void img_from_model_kernel(const float *__restrict__ model, int m1, i
                                       int f1, int f2, int f3, float *__restrict__ img, int n1,
                                       int n2, int n3, int pitch) {
   const long long total = (long long)n1 * n2 * n3;
+  const bool narrow = total < (1LL << 31);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(t % n1), y = (int)((t / n1) % n2), z = (int)(t / ((long long)n1 * n2));
+    int x, y;
+    const int z = (int)divmod(divmod(t, n1, narrow, x), n2, narrow, y);
     const int mx = x + f1, my = y + f2;
     auto e = [&](int zz) -> float {
       const int mz = zz + f3;
@@ -41,9 +56,11 @@ __global__ void model_from_img_kernel(float *__restrict__ model, int m1, int m2,
                                       int f2, int f3, const float *__restrict__ img, int n1, int n2,
                                       int n3, int pitch) {
   const long long total = (long long)m1 * m2 * m3;
+  const bool narrow = total < (1LL << 31);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int mx = (int)(t % m1), my = (int)((t / m1) % m2), mz = (int)(t / ((long long)m1 * m2));
+    int mx, my;
+    const int mz = (int)divmod(divmod(t, m1, narrow, mx), m2, narrow, my);
     const int x = mx - f1, y = my - f2, z = mz - f3;
     if (x < 0 || x >= n1 || y < 0 || y >= n2 || z < 0 || z >= n3) continue;
     const long long i = x + (long long)pitch * (y + (long long)n2 * z);
@@ -60,9 +77,11 @@ __global__ void model_from_img_kernel(float *__restrict__ model, int m1, int m2,
 __global__ void data_from_traces_kernel(const float *__restrict__ trc, int nrec, int rnx, int nt,
                                         float dt, float *__restrict__ data) {
   const long long total = (long long)nrec * nt;
+  const bool narrow = total < (1LL << 31);
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
        k += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(k / nt), t = (int)(k % nt);
+    int t;
+    const int r = (int)divmod(k, nt, narrow, t);
     const bool first = (r % rnx) == 0;
     auto m = [&](int rr, int tt) { return __fdiv_rn(trc[(long long)(tt + 4) * nrec + rr], dt); };
     float v;
@@ -87,9 +106,11 @@ __global__ void data_from_traces_kernel(const float *__restrict__ trc, int nrec,
 __global__ void traces_from_data_kernel(const float *__restrict__ data, int nrec, int rnx, int nt,
                                         int ntrace, float dt, float *__restrict__ trc) {
   const long long total = (long long)nrec * ntrace;
+  const bool narrow = total < (1LL << 31);
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
        k += (long long)gridDim.x * blockDim.x) {
-    const int s = (int)(k / nrec), r = (int)(k % nrec);   // time-major output index
+    int r;
+    const int s = (int)divmod(k, nrec, narrow, r);   // time-major output index
     const int t = s - 4;
     float v = 0.f;
     if (t >= 0 && t < nt) {

@@ -967,16 +967,43 @@ __global__ void __launch_bounds__(256) wgrad1x1_kernel(View x, View dy, long lon
 // Memory-bound pieces.
 // ---------------------------------------------------------------------------
 // 2x2x2 average pooling: out (D/2, H/2, W/2)
+// element e of a walk over (voxel, 8-channel group) of an nb x D x H x W
+// volume -> group g, voxel v and its coordinates.  32-bit divisions where the
+// walk is shorter than 2^31 (every U-Net volume): several times cheaper than
+// the 64-bit ones, and these kernels are otherwise bound by them.
+struct EV {
+  long long v;
+  int g, n, z, y, x;
+};
+template <typename I>
+__device__ __forceinline__ EV decode_ev_t(I e, int cg, int D, int H, int W) {
+  EV r;
+  const I v = e / (I)cg;
+  r.g = (int)(e - v * (I)cg);
+  const I q1 = v / (I)W;
+  r.x = (int)(v - q1 * (I)W);
+  const I q2 = q1 / (I)H;
+  r.y = (int)(q1 - q2 * (I)H);
+  const I q3 = q2 / (I)D;
+  r.z = (int)(q2 - q3 * (I)D);
+  r.n = (int)q3;
+  r.v = (long long)v;
+  return r;
+}
+__device__ __forceinline__ EV decode_ev(long long e, bool narrow, int cg, int D, int H, int W) {
+  return narrow ? decode_ev_t<uint32_t>((uint32_t)e, cg, D, H, W) : decode_ev_t<long long>(e, cg, D, H, W);
+}
+
 __global__ void avgpool_kernel(View x, int nb, int D, int H, int W, int c, __nv_bfloat16 *y,
                                int y_cstride, int y_coff) {
   const int D2 = D / 2, H2 = H / 2, W2 = W / 2, cg = c / 8;
   const long long total = (long long)nb * D2 * H2 * W2 * cg;
+  const bool narrow = total < (1LL << 31);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % cg);
-    long long v = e / cg;
-    const int xx = (int)(v % W2), yy = (int)((v / W2) % H2), zz = (int)((v / ((long long)W2 * H2)) % D2);
-    const int n = (int)(v / ((long long)W2 * H2 * D2));
+    const EV c4 = decode_ev(e, narrow, cg, D2, H2, W2);
+    const int g = c4.g, xx = c4.x, yy = c4.y, zz = c4.z, n = c4.n;
+    const long long v = c4.v;
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int d = 0; d < 8; d++) {
       const long long vi = (((long long)n * D + 2 * zz + (d >> 2)) * H + 2 * yy + ((d >> 1) & 1)) * W +
@@ -998,12 +1025,12 @@ __global__ void avgpool_bwd_kernel(View dy, int nb, int D, int H, int W, int c, 
                                    int dx_cstride, int dx_coff, int accumulate, View mask) {
   const int D2 = D / 2, H2 = H / 2, W2 = W / 2, cg = c / 8;
   const long long total = (long long)nb * D * H * W * cg;
+  const bool narrow = total < (1LL << 31);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % cg);
-    const long long v = e / cg;
-    const int xx = (int)(v % W), yy = (int)((v / W) % H), zz = (int)((v / ((long long)W * H)) % D);
-    const int n = (int)(v / ((long long)W * H * D));
+    const EV c4 = decode_ev(e, narrow, cg, D, H, W);
+    const int g = c4.g, xx = c4.x, yy = c4.y, zz = c4.z, n = c4.n;
+    const long long v = c4.v;
     const long long vp = (((long long)n * D2 + zz / 2) * H2 + yy / 2) * W2 + xx / 2;
     const uint4 q = *reinterpret_cast<const uint4 *>(dy.p + vp * dy.cstride + dy.coff + g * 8);
     const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
@@ -1031,12 +1058,12 @@ __global__ void upsample_kernel(View x, int nb, int D, int H, int W, int c, __nv
   const int cg = c / 8;
   const int D2 = 2 * D, H2 = 2 * H, W2 = 2 * W;
   const long long total = (long long)nb * D2 * H2 * W2 * cg;
+  const bool narrow = total < (1LL << 31);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % cg);
-    const long long v = e / cg;
-    const int xx = (int)(v % W2), yy = (int)((v / W2) % H2), zz = (int)((v / ((long long)W2 * H2)) % D2);
-    const int n = (int)(v / ((long long)W2 * H2 * D2));
+    const EV c4 = decode_ev(e, narrow, cg, D2, H2, W2);
+    const int g = c4.g, xx = c4.x, yy = c4.y, zz = c4.z, n = c4.n;
+    const long long v = c4.v;
     const long long vs = (((long long)n * D + zz / 2) * H + yy / 2) * W + xx / 2;
     *reinterpret_cast<uint4 *>(y + v * y_cstride + y_coff + g * 8) =
         *reinterpret_cast<const uint4 *>(x.p + vs * x.cstride + x.coff + g * 8);
@@ -1048,12 +1075,12 @@ __global__ void upsample_bwd_kernel(View dy, int nb, int D, int H, int W, int c,
                                     int dx_cstride, int dx_coff, View mask) {
   const int cg = c / 8;
   const long long total = (long long)nb * D * H * W * cg;
+  const bool narrow = total < (1LL << 31);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % cg);
-    const long long v = e / cg;
-    const int xx = (int)(v % W), yy = (int)((v / W) % H), zz = (int)((v / ((long long)W * H)) % D);
-    const int n = (int)(v / ((long long)W * H * D));
+    const EV c4 = decode_ev(e, narrow, cg, D, H, W);
+    const int g = c4.g, xx = c4.x, yy = c4.y, zz = c4.z, n = c4.n;
+    const long long v = c4.v;
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int d = 0; d < 8; d++) {
       const long long vc = (((long long)n * 2 * D + 2 * zz + (d >> 2)) * 2 * H + 2 * yy + ((d >> 1) & 1)) *
@@ -1082,10 +1109,11 @@ __global__ void relu_mask_kernel(View y, __nv_bfloat16 *dy, int dy_cstride, int 
                                  int c) {
   const int cg = c / 8;
   const long long total = V * cg;
+  const bool narrow = total < (1LL << 31);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % cg);
-    const long long v = e / cg;
+    const long long v = narrow ? (long long)((uint32_t)e / (uint32_t)cg) : e / cg;
+    const int g = (int)(e - v * cg);
     const uint4 qy = *reinterpret_cast<const uint4 *>(y.p + v * y.cstride + y.coff + g * 8);
     __nv_bfloat16 *dst = dy + v * dy_cstride + dy_coff + g * 8;
     uint4 qd = *reinterpret_cast<const uint4 *>(dst);
