@@ -95,15 +95,17 @@ __global__ void repitch_kernel(const float *__restrict__ src, long long spitch, 
   if (vec4) {
     const int w4 = width >> 2;
     const long long n = rows * w4;
+    const bool narrow = n < (1LL << 31);   // 32-bit division (uniform per launch)
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-      const long long r = i / w4, c = i - r * w4;
+      const long long r = narrow ? (long long)((uint32_t)i / (uint32_t)w4) : i / w4, c = i - r * w4;
       const float4 v = __ldcs(reinterpret_cast<const float4 *>(src + r * spitch) + c);
       __stcs(reinterpret_cast<float4 *>(dst + r * dpitch) + c, v);
     }
   } else {
     const long long n = rows * width;
+    const bool narrow = n < (1LL << 31);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-      const long long r = i / width, c = i - r * width;
+      const long long r = narrow ? (long long)((uint32_t)i / (uint32_t)width) : i / width, c = i - r * width;
       dst[r * dpitch + c] = __ldcs(src + r * spitch + c);
     }
   }
