@@ -13,8 +13,13 @@
 //
 // GEMM shapes: forward / data gradient  M = voxels (tiles of 128),
 // N = output channels (16..128), K = taps x input channels (chunks of 64);
-// weight gradient  M = taps x input channels (tiles of 128), N = output
-// channels, K = voxels (chunks of 64, split over CTAs, FP32 atomics).
+// weight gradient of the narrow layers (sepx_unet_wgrad.inc): M = (x shift,
+// output channel), N = (y shift, input channel), K = the 128 voxels of a
+// tile, nine taps per MMA; of the others (gather kernel below): M = taps x
+// input channels (tiles of 128), N = output channels, K = voxels (chunks of
+// 64, split over CTAs).  Both write per-CTA partial sums that a second kernel
+// adds in a fixed order (the gather kernel adds with FP32 atomics only when
+// the halo-staged kernels are switched off).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -1802,8 +1807,7 @@ int sepx_unet_conv_wgrad_bias(const void *x, int x_cstride, int x_coff, int nb, 
   const long long vchunks = (V + kKC - 1) / kKC;
   const int mt = (ntap * cin + kTM - 1) / kTM;
   // enough CTAs to fill the GPU about twice, with at least 16 voxel chunks
-  // each (fewer on the smallest volumes: at least 4, and 8 splits); every
-  // split adds its sums with FP32 atomics, so more splits cost contention
+  // each (fewer on the smallest volumes: at least 4, and 8 splits)
   long long per = (vchunks * mt + 2 * 152 * 4 - 1) / (2 * 152 * 4);
   per = std::max(per, std::max(4LL, std::min(16LL, vchunks / 8)));
   // with the halo-staged kernels on, each split writes its sums to a partial
