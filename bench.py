@@ -41,8 +41,8 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nt", type=int, default=4000, help="propagation steps (the workload's 4000)")
     p.add_argument("--grid", default="512x512x400")
-    # 25 steps of each loop on the full grid: about 13 s of CPU work on 16 cores
-    p.add_argument("--cpu-sample-steps", type=int, default=25)
+    # a 100-step window of each loop on the full grid
+    p.add_argument("--cpu-sample-steps", type=int, default=100)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--e2e-clock-ms", type=int, default=1000,
                    help="nvidia-smi sampling interval during the e2e region (0: none)")
@@ -484,7 +484,7 @@ def run_reference(args, ws, rank):
     orc = Oracle()
     s, st = build_workload_oracle(args, orc)
     for _ in range(args.warmup):
-        cpu_baseline(s, st, max(1, args.cpu_sample_steps // 2), orc)
+        cpu_baseline(s, st, max(1, args.cpu_sample_steps // 10), orc)
     vals = []
     secs = 0.0
     for _ in range(args.steps):
