@@ -18,6 +18,7 @@ import pytest
 
 from sep_code_gb300 import gpu_funcs as gf
 from sep_code_gb300 import model as M
+from tests.golden.make_golden import CASES as GOLDEN_CASES
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -170,11 +171,10 @@ def _python_born_forward(oracle, s):
     return st, data
 
 
-@pytest.mark.parametrize("case", ["small", "jt2"])
+@pytest.mark.parametrize("case", list(GOLDEN_CASES))
 def test_reference_operator_forward(case, oracle, refhost):
     from oracle.bindings import RefOperator
-    s = M.small_survey() if case == "small" else \
-        M.small_survey(m1=20, m2=20, m3=20, nt=30, seed=3, data_dt=0.004, dtw=0.004)
+    s = M.small_survey(**GOLDEN_CASES[case])
     ref = RefOperator(refhost)
     d_ref = ref.born_forward(s)
     st, d_py = _python_born_forward(oracle, s)
