@@ -72,18 +72,22 @@ def _newer(target: Path, deps: list[Path]) -> bool:
     return all(d.stat().st_mtime <= t for d in deps if d.exists())
 
 
-def build_oracle(force: bool = False) -> Path:
-    BUILD.mkdir(exist_ok=True)
+def build_oracle(force: bool = False, out: Path | None = None, defines: tuple = ()) -> Path:
+    """The oracle library; ``out`` / ``defines`` build a variant elsewhere
+    (tests: the stencil block sizes OZB / OYB)."""
+    target = ORACLE_SO if out is None else Path(out)
+    target.parent.mkdir(parents=True, exist_ok=True)
     deps = [HERE / "sepx_oracle.c", HERE / "sepx_oracle.h", HERE / "sepx_oracle_loops.inc",
             Path(__file__)]
-    if not force and _newer(ORACLE_SO, deps):
-        return ORACLE_SO
+    if not force and not defines and _newer(target, deps):
+        return target
     cmd = ["gcc", "-std=gnu11", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-math-errno",
            "-fPIC", "-shared", *_arch_flags(), "-Wall", "-Wno-unused-function",
-           str(HERE / "sepx_oracle.c"), "-o", str(ORACLE_SO) + ".tmp", "-lm"]
+           *[f"-D{d}" for d in defines],
+           str(HERE / "sepx_oracle.c"), "-o", str(target) + ".tmp", "-lm"]
     subprocess.run(cmd, check=True)
-    os.replace(str(ORACLE_SO) + ".tmp", ORACLE_SO)
-    return ORACLE_SO
+    os.replace(str(target) + ".tmp", target)
+    return target
 
 
 def build_ref(force: bool = False) -> Path | None:
