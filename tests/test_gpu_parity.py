@@ -24,6 +24,8 @@ def _cases():
         "ragged": dict(m1=37, m2=23, m3=21, nt=40, seed=11),
         # data sampled at twice the propagation step: two-row sinc tables
         "jt2": dict(m1=20, m2=20, m3=20, nt=30, seed=3, data_dt=0.004, dtw=0.004),
+        # three propagation steps per data sample: three-row sinc tables
+        "jt3": dict(m1=20, m2=20, m3=20, nt=20, seed=3, data_dt=0.006, dtw=0.006),
     }
 
 
@@ -112,6 +114,30 @@ def test_short_loops(oracle):
         g = GpuShot(s, st).rtm_adjoint(p0, p1, traces)
         o = OracleShot(oracle, s, st).rtm_adjoint(p0, p1, traces)
         assert np.array_equal(g, o), nt_data
+
+
+def test_short_source_prop_and_one_receiver(oracle):
+    """source_prop of nt = 1 and 2 data samples (nt+1 steps), and all three
+    loops with a single receiver (a 1 x 1 receiver grid), bit for bit."""
+    for nt_data in (1, 2):
+        s = M.small_survey(m1=20, m2=20, m3=20, nt=nt_data, seed=8)
+        st = M.prepare_shot(s)
+        g = GpuShot(s, st).source_prop()
+        o = OracleShot(oracle, s, st).source_prop()
+        for a, b in zip(g, o):
+            assert np.array_equal(a, b), nt_data
+    s = M.small_survey(m1=24, m2=20, m3=28, nt=30, seed=4, rnx=1, rny=1)
+    st = M.prepare_shot(s)
+    gs, os_ = GpuShot(s, st), OracleShot(oracle, s, st)
+    gp, op = gs.source_prop(), os_.source_prop()
+    assert all(np.array_equal(a, b) for a, b in zip(gp, op))
+    gt, ot = gs.rtm_forward(st.img_lap), os_.rtm_forward(st.img_lap)
+    assert gt.shape == (1, st.nt_big) and np.abs(ot).max() > 0
+    assert np.array_equal(gt, ot)
+    gi = gs.rtm_adjoint(op[1], op[0], ot)
+    oi = os_.rtm_adjoint(op[1], op[0], ot)
+    assert np.abs(oi).max() > 0
+    assert np.array_equal(gi, oi)
 
 
 def test_errors_are_reported():
